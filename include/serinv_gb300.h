@@ -1,0 +1,158 @@
+/*
+ * serinv_gb300 — C ABI of the GB300 (sm_103a) implementation of the
+ * sequential block-tridiagonal-with-arrowhead (BTA) hot path:
+ *
+ *   sgb_pobtaf   block Cholesky            (replaces serinv.algs.pobtaf)
+ *   sgb_pobtasi  selected inversion        (replaces serinv.algs.pobtasi)
+ *   sgb_pobtas   block triangular solve    (replaces serinv.algs.pobtas)
+ *
+ * The reference is a Python library without an FFI; each entry point below
+ * takes the place of one of its public functions, with the same in-place
+ * block-stack layout (C-contiguous, row-major):
+ *
+ *   diag  (n, b, b)   A_diagonal_blocks        lower triangle meaningful
+ *   lower (n-1, b, b) A_lower_diagonal_blocks  lower[i] = A[i+1, i]
+ *   arrow (n, a, b)   A_lower_arrow_blocks     arrow[i] = A[tip, i]
+ *   tip   (a, a)      A_arrow_tip_block
+ *   rhs   (n*b + a, nrhs)
+ *
+ * All pointers are device pointers (or memory the GPU can address).  Every
+ * call is asynchronous on `stream` (a cudaStream_t, 0 = legacy default
+ * stream) and allocates nothing: scratch memory comes from the caller as a
+ * workspace whose size the matching *_workspace_size query returns.  The
+ * return code reports argument and launch errors immediately; a non-SPD
+ * pivot is reported on the device through `info` (see below) because it is
+ * only known once the kernels have run.
+ *
+ * Thread safety: calls on different streams with disjoint arrays and
+ * workspaces may run concurrently.
+ */
+#ifndef SERINV_GB300_H
+#define SERINV_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes --------------------------------------------------- */
+#define SGB_OK               0
+#define SGB_ERR_SHAPE        1  /* n < 1, b < 1, a < 0, nrhs < 0, or sizes too large   */
+#define SGB_ERR_DTYPE        2  /* dtype not SGB_F32 / SGB_F64                          */
+#define SGB_ERR_NOT_SPD      3  /* reported through *info on the device, never returned */
+#define SGB_ERR_TIMEOUT      4  /* a bounded device wait gave up                        */
+#define SGB_ERR_CUDA         5  /* a CUDA runtime call failed (sgb_last_cuda_error)    */
+#define SGB_ERR_WORKSPACE    6  /* workspace missing, too small or misaligned          */
+#define SGB_ERR_ARG          7  /* null pointer, bad trans, bad precision              */
+#define SGB_ERR_UNSUPPORTED  8  /* valid request this build does not implement         */
+
+/* ---- element types -------------------------------------------------- */
+#define SGB_F32 0
+#define SGB_F64 1
+
+/* ---- precision modes ------------------------------------------------ */
+/* Arithmetic in the storage type throughout: the drop-in form. */
+#define SGB_PREC_NATIVE 0
+/* FP64 storage; the dense block products run on the tensor cores as exact
+ * bf16 slice products (fixed-point split of each FP64 operand) accumulated
+ * in FP32 and summed in FP64; diagonal pivots stay in FP64.               */
+#define SGB_PREC_MIXED  1
+
+typedef struct sgb_bta {
+    int32_t dtype;     /* SGB_F32 or SGB_F64                       */
+    int32_t _pad;
+    int64_t n;         /* number of diagonal blocks, >= 1          */
+    int64_t b;         /* diagonal block size, >= 1                */
+    int64_t a;         /* arrowhead width, >= 0                    */
+    void* diag;        /* (n, b, b)                                */
+    void* lower;       /* (n-1, b, b); may be NULL when n == 1     */
+    void* arrow;       /* (n, a, b);  may be NULL when a == 0      */
+    void* tip;         /* (a, a);     may be NULL when a == 0      */
+} sgb_bta;
+
+/* Library version as 10000*major + 100*minor + patch. */
+int sgb_version(void);
+
+/* Static description of a return code. */
+const char* sgb_strerror(int code);
+
+/* The cudaError_t of the last SGB_ERR_CUDA returned on this thread. */
+int sgb_last_cuda_error(void);
+
+/*
+ * Workspace sizes in bytes for one call with these shapes.  The workspace
+ * must be device memory aligned to 256 bytes.
+ */
+int sgb_pobtaf_workspace_size(const sgb_bta* m, int precision, size_t* bytes);
+int sgb_pobtasi_workspace_size(const sgb_bta* m, int precision, size_t* bytes);
+int sgb_pobtas_workspace_size(const sgb_bta* m, int64_t nrhs, int precision, size_t* bytes);
+
+/*
+ * In-place block Cholesky A = L L^T.
+ * Replaces serinv.algs.pobtaf (src/serinv/algs/pobtaf.py:11-94, natural
+ * ordering _pobtaf :97-183).  On return (stream order) diag holds L_ii with
+ * a zero strict upper triangle, lower holds L_{i+1,i}, arrow holds L_{a,i},
+ * tip holds L_tip (zero strict upper triangle).
+ * factorize_last_block == 0 leaves the last diagonal block and the tip
+ * updated but not factorized (pobtaf.py:161).
+ * info: device int32 set to 0 at the start of the call and, if a pivot is
+ * not positive (or not finite), to the 1-based global row of the first such
+ * pivot, like LAPACK potrf.  May be NULL.
+ */
+int sgb_pobtaf(const sgb_bta* m, int factorize_last_block, int precision,
+               void* workspace, size_t workspace_bytes, int32_t* info,
+               void* stream);
+
+/*
+ * In-place selected inversion from the factor of sgb_pobtaf.
+ * Replaces serinv.algs.pobtasi (src/serinv/algs/pobtasi.py:10-89, natural
+ * ordering _pobtasi :92-172).  On return diag holds X_ii (full, symmetric),
+ * lower holds X_{i+1,i}, arrow holds X_{a,i}, tip holds X_tip: the blocks of
+ * A^{-1} on the BTA pattern.  invert_last_block == 0 takes the last diagonal
+ * block, the last arrow block and the tip as already inverted
+ * (pobtasi.py:114).
+ */
+int sgb_pobtasi(const sgb_bta* m, int invert_last_block, int precision,
+                void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * In-place block triangular solve with the factor of sgb_pobtaf.
+ * Replaces serinv.algs.pobtas (src/serinv/algs/pobtas.py:10-62, natural
+ * ordering _pobtas :65-161): trans 'N' computes B <- L^{-1} B, 'T' or 'C'
+ * computes B <- L^{-T} B.  rhs is (n*b + a, nrhs) row-major with leading
+ * dimension ldb >= nrhs.  partial != 0 skips the last diagonal block and the
+ * tip (pobtas.py:99,129).  For a == 0 the call is the arrow-free solve
+ * (src/serinv/algs/pobts.py:57-118).
+ */
+int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char trans,
+               int partial, int precision, void* workspace, size_t workspace_bytes,
+               void* stream);
+
+/* ---- diagnostics (no counterpart in the reference) -------------------- */
+
+/* Kernel classes for sgb_profile_read. */
+#define SGB_KCLASS_GEMM        0  /* grouped block products (SIMT FP64/FP32)   */
+#define SGB_KCLASS_POTRF_TILE  1  /* diagonal-tile Cholesky + tile inverse     */
+#define SGB_KCLASS_TRTRI_TILE  2  /* diagonal-tile triangular inverses         */
+#define SGB_KCLASS_GEMM_TC     3  /* tensor-core (tcgen05) block products      */
+#define SGB_KCLASS_SPLIT       4  /* operand slicing for the tensor-core path  */
+#define SGB_KCLASS_COUNT       5
+
+/* Number of kernels this library has launched since it was loaded. */
+long long sgb_launch_count(void);
+
+/* Enable (1) or disable (0) per-launch CUDA-event timing; clears records. */
+int sgb_profile_enable(int on);
+
+/* Totals over the recorded launches of one class: launch count, device
+ * milliseconds between the events bracketing each launch, and algorithmic
+ * flops (useful multiply-adds x 2).  Synchronises on the recorded events. */
+int sgb_profile_read(int kclass, long long* launches, double* ms, double* flops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SERINV_GB300_H */

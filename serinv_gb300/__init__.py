@@ -1,0 +1,13 @@
+"""serinv_gb300 — GB300-native BTA Cholesky, selected inversion and solve.
+
+Drop-in for the sequential hot path of serinv (``serinv.algs.pobtaf``,
+``pobtasi``, ``pobtas``): same call signatures and in-place block-stack
+layout, computed by hand-written sm_103a CUDA kernels behind the C ABI in
+``include/serinv_gb300.h``.
+"""
+
+__version__ = "0.1.0"
+
+from .algs import pobtaf, pobtasi, pobtas  # noqa: E402,F401
+
+__all__ = ["pobtaf", "pobtasi", "pobtas", "__version__"]

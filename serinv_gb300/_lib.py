@@ -1,0 +1,152 @@
+"""ctypes binding of ``libserinv_gb300.so`` (the C ABI in include/serinv_gb300.h).
+
+The library is built in-tree by ``serinv_gb300.build``.  Loading fails loudly
+when it is missing: there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+SGB_OK = 0
+SGB_ERR_SHAPE = 1
+SGB_ERR_DTYPE = 2
+SGB_ERR_NOT_SPD = 3
+SGB_ERR_TIMEOUT = 4
+SGB_ERR_CUDA = 5
+SGB_ERR_WORKSPACE = 6
+SGB_ERR_ARG = 7
+SGB_ERR_UNSUPPORTED = 8
+
+SGB_F32 = 0
+SGB_F64 = 1
+
+SGB_PREC_NATIVE = 0
+SGB_PREC_MIXED = 1
+
+PRECISIONS = {"native": SGB_PREC_NATIVE, "fp64": SGB_PREC_NATIVE, "mixed": SGB_PREC_MIXED}
+
+
+class SgbBta(ctypes.Structure):
+    _fields_ = [
+        ("dtype", ctypes.c_int32),
+        ("_pad", ctypes.c_int32),
+        ("n", ctypes.c_int64),
+        ("b", ctypes.c_int64),
+        ("a", ctypes.c_int64),
+        ("diag", ctypes.c_void_p),
+        ("lower", ctypes.c_void_p),
+        ("arrow", ctypes.c_void_p),
+        ("tip", ctypes.c_void_p),
+    ]
+
+
+# name -> (restype, argtypes)
+_SIGNATURES = {
+    "sgb_version": (ctypes.c_int, []),
+    "sgb_strerror": (ctypes.c_char_p, [ctypes.c_int]),
+    "sgb_last_cuda_error": (ctypes.c_int, []),
+    "sgb_pobtaf_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int,
+                                                 ctypes.POINTER(ctypes.c_size_t)]),
+    "sgb_pobtasi_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int,
+                                                  ctypes.POINTER(ctypes.c_size_t)]),
+    "sgb_pobtas_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int64, ctypes.c_int,
+                                                 ctypes.POINTER(ctypes.c_size_t)]),
+    "sgb_pobtaf": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                  ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
+    "sgb_pobtasi": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                   ctypes.c_size_t, ctypes.c_void_p]),
+    "sgb_pobtas": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                  ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                  ctypes.c_size_t, ctypes.c_void_p]),
+    "sgb_launch_count": (ctypes.c_longlong, []),
+    "sgb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
+    "sgb_profile_read": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
+                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+}
+
+KCLASS = {"gemm": 0, "potrf_tile": 1, "trtri_tile": 2, "gemm_tc": 3, "split": 4}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIBPATH
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load the shared library (building it first if it is absent)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = lib_path()
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise RuntimeError(f"serinv_gb300: {path} is not built")
+            _build.build()
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def exported_symbols():
+    return list(_SIGNATURES)
+
+
+def launch_count() -> int:
+    """Kernels launched by the library since it was loaded."""
+    return int(load().sgb_launch_count())
+
+
+def profile_enable(on: bool) -> None:
+    load().sgb_profile_enable(1 if on else 0)
+
+
+def profile_read() -> dict:
+    """Per kernel class: launches, device ms, algorithmic flops (synchronises)."""
+    lib = load()
+    out = {}
+    for name, k in KCLASS.items():
+        n = ctypes.c_longlong(0)
+        ms = ctypes.c_double(0)
+        fl = ctypes.c_double(0)
+        raise_for(lib.sgb_profile_read(k, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(fl)), "profile")
+        if n.value:
+            out[name] = {"launches": n.value, "ms": ms.value, "flops": fl.value}
+    return out
+
+
+class SgbError(RuntimeError):
+    pass
+
+
+def raise_for(code: int, what: str) -> None:
+    """Map a C return code to the exception type the reference would raise."""
+    if code == SGB_OK:
+        return
+    lib = load()
+    msg = f"{what}: {lib.sgb_strerror(code).decode()}"
+    if code == SGB_ERR_CUDA:
+        msg += f" (cudaError {lib.sgb_last_cuda_error()})"
+        raise SgbError(msg)
+    if code in (SGB_ERR_SHAPE, SGB_ERR_ARG):
+        raise ValueError(msg)
+    if code == SGB_ERR_DTYPE:
+        raise TypeError(msg)
+    if code == SGB_ERR_NOT_SPD:
+        raise np.linalg.LinAlgError(msg)
+    if code == SGB_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    raise SgbError(msg)

@@ -1,0 +1,284 @@
+"""Drop-in ``pobtaf`` / ``pobtasi`` / ``pobtas`` running on the GB300 kernels.
+
+Same names, positional arguments, keyword arguments, in-place semantics and
+exception types as the reference's sequential functions:
+
+* ``pobtaf``  — src/serinv/algs/pobtaf.py:11-94
+* ``pobtasi`` — src/serinv/algs/pobtasi.py:10-89
+* ``pobtas``  — src/serinv/algs/pobtas.py:10-62
+
+Arrays may be torch tensors (CUDA or CPU), NumPy arrays, or any CUDA array
+exporting ``__dlpack__`` (CuPy).  Device arrays are used in place on the
+current torch stream; host arrays are copied to the GPU, processed, and
+copied back in place (the whole matrix fits in HBM, so the reference's
+``device_streaming`` mode needs no separate code path and is accepted as a
+no-op).  All arithmetic runs in ``libserinv_gb300.so``; if it cannot be
+loaded or no GPU is present, the call raises — there is no CPU fallback.
+
+Extensions (keyword-only, absent from the reference): ``precision`` —
+``"fp64"`` (default, arithmetic in the storage type) or ``"mixed"``;
+``check_spd`` (pobtaf, default True) — synchronise and raise
+``numpy.linalg.LinAlgError`` on a non-positive pivot, like SciPy's
+``cholesky`` in the reference.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_POBTAF_KW = {"device_streaming", "buffer", "factorize_last_block"}   # pobtaf.py:50
+_POBTASI_KW = {"device_streaming", "buffer", "invert_last_block"}     # pobtasi.py:45
+_EXTENSION_KW = {"precision", "check_spd"}
+
+
+# --------------------------------------------------------------------------
+# array plumbing
+
+
+class _Arr:
+    """A CUDA, C-contiguous torch view of a user array plus its write-back."""
+
+    __slots__ = ("t", "src", "kind")
+
+    def __init__(self, t: torch.Tensor, src, kind: str):
+        self.t = t
+        self.src = src
+        self.kind = kind  # "dev" (shared storage), "devcopy", "torch_host", "numpy"
+
+    def writeback(self) -> None:
+        if self.kind == "devcopy":
+            self.src.copy_(self.t)
+        elif self.kind == "torch_host":
+            self.src.copy_(self.t.to("cpu"))
+        elif self.kind == "numpy":
+            host = self.t.to("cpu").numpy()
+            np.copyto(self.src, host.reshape(self.src.shape), casting="no")
+
+
+def _device_of(arrs) -> torch.device:
+    for x in arrs:
+        if isinstance(x, torch.Tensor) and x.is_cuda:
+            return x.device
+    if not torch.cuda.is_available():
+        raise RuntimeError("serinv_gb300 needs a CUDA GPU; none is available (no CPU fallback)")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _wrap(x, device: torch.device, name: str) -> _Arr:
+    if isinstance(x, torch.Tensor):
+        if x.is_cuda:
+            if x.device != device:
+                raise ValueError(f"{name} is on {x.device}, expected {device}")
+            if x.is_contiguous():
+                return _Arr(x, x, "dev")
+            return _Arr(x.contiguous(), x, "devcopy")
+        return _Arr(x.to(device).contiguous(), x, "torch_host")
+    if isinstance(x, np.ndarray):
+        if not x.flags.writeable:
+            raise ValueError(f"{name} is read-only; the computation is in place")
+        return _Arr(torch.from_numpy(np.ascontiguousarray(x)).to(device), x, "numpy")
+    if hasattr(x, "__dlpack__"):
+        t = torch.from_dlpack(x)
+        if not t.is_cuda:
+            return _Arr(t.to(device).contiguous(), t, "torch_host")
+        if t.device != device:
+            raise ValueError(f"{name} is on {t.device}, expected {device}")
+        if t.is_contiguous():
+            return _Arr(t, t, "dev")
+        return _Arr(t.contiguous(), t, "devcopy")
+    raise TypeError(f"{name}: unsupported array type {type(x).__name__}")
+
+
+def _dtype_code(dt: torch.dtype) -> int:
+    if dt == torch.float64:
+        return _lib.SGB_F64
+    if dt == torch.float32:
+        return _lib.SGB_F32
+    if dt in (torch.complex64, torch.complex128):
+        raise NotImplementedError("complex BTA matrices are not supported yet")
+    raise TypeError(f"unsupported dtype {dt}")
+
+
+def _ptr(t: torch.Tensor):
+    return t.data_ptr() if t.numel() > 0 else None
+
+
+def _bta_struct(D, Lo, Ar, T):
+    """Validate the four stacks and build the C descriptor."""
+    if D.dim() != 3 or D.shape[1] != D.shape[2]:
+        raise ValueError(f"diagonal blocks must have shape (n, b, b), got {tuple(D.shape)}")
+    n, b = D.shape[0], D.shape[1]
+    if Ar.dim() != 3 or Ar.shape[0] != n or Ar.shape[2] != b:
+        raise ValueError(f"arrow blocks must have shape (n, a, b) = ({n}, a, {b}), got {tuple(Ar.shape)}")
+    a = Ar.shape[1]
+    if Lo.dim() != 3 or tuple(Lo.shape) != (n - 1, b, b):
+        raise ValueError(f"lower blocks must have shape ({n - 1}, {b}, {b}), got {tuple(Lo.shape)}")
+    if tuple(T.shape) != (a, a):
+        raise ValueError(f"arrow tip must have shape ({a}, {a}), got {tuple(T.shape)}")
+    if n < 1 or b < 1:
+        raise ValueError("need at least one diagonal block of size >= 1")
+    dts = {D.dtype, Lo.dtype, Ar.dtype, T.dtype}
+    if len(dts) != 1:
+        raise TypeError(f"all blocks must share one dtype, got {sorted(map(str, dts))}")
+    m = _lib.SgbBta()
+    m.dtype = _dtype_code(D.dtype)
+    m.n, m.b, m.a = n, b, a
+    m.diag, m.lower, m.arrow, m.tip = _ptr(D), _ptr(Lo), _ptr(Ar), _ptr(T)
+    return m
+
+
+def _precision(kwargs) -> int:
+    p = kwargs.get("precision", "fp64")
+    if p not in _lib.PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(_lib.PRECISIONS)}, got {p!r}")
+    return _lib.PRECISIONS[p]
+
+
+def _workspace(nbytes: int, device) -> torch.Tensor:
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)
+
+
+def _stream(device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _prepare(arrays, names):
+    device = _device_of(arrays)
+    wrapped = [_wrap(x, device, nm) for x, nm in zip(arrays, names)]
+    return device, wrapped
+
+
+def _finish(wrapped) -> None:
+    host = any(w.kind in ("numpy", "torch_host") for w in wrapped)
+    for w in wrapped:
+        w.writeback()
+    if host:
+        torch.cuda.current_stream(wrapped[0].t.device).synchronize()
+
+
+# --------------------------------------------------------------------------
+# public API
+
+
+def pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_arrow_tip_block, **kwargs):
+    """Cholesky factorization of a block tridiagonal with arrowhead SPD matrix, in place.
+
+    Mirrors src/serinv/algs/pobtaf.py:11-94.  Keyword arguments:
+    ``device_streaming`` (accepted; the matrix is processed in HBM),
+    ``buffer`` (permuted middle-partition variant, pobtaf.py:186-281: not
+    supported yet, raises NotImplementedError), ``factorize_last_block``
+    (default True).  Unknown keywords raise TypeError (pobtaf.py:50-53).
+    """
+    unexpected = set(kwargs) - _POBTAF_KW - _EXTENSION_KW
+    if unexpected:
+        raise TypeError(f"Unexpected keyword arguments: {unexpected}")
+    if kwargs.get("buffer", None) is not None:
+        raise NotImplementedError("the permuted (buffer=) factorization is not supported yet")
+    factorize_last_block = bool(kwargs.get("factorize_last_block", True))
+    precision = _precision(kwargs)
+    check = bool(kwargs.get("check_spd", True))
+
+    lib = _lib.load()
+    device, w = _prepare(
+        (A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_arrow_tip_block),
+        ("A_diagonal_blocks", "A_lower_diagonal_blocks", "A_lower_arrow_blocks", "A_arrow_tip_block"))
+    m = _bta_struct(*(x.t for x in w))
+    with torch.cuda.device(device):
+        nbytes = ctypes.c_size_t(0)
+        _lib.raise_for(lib.sgb_pobtaf_workspace_size(ctypes.byref(m), precision, ctypes.byref(nbytes)),
+                       "pobtaf")
+        ws = _workspace(nbytes.value, device)
+        info = torch.zeros(1, dtype=torch.int32, device=device)
+        rc = lib.sgb_pobtaf(ctypes.byref(m), int(factorize_last_block), precision, ws.data_ptr(),
+                            nbytes.value, info.data_ptr(), _stream(device))
+        _lib.raise_for(rc, "pobtaf")
+        _finish(w)
+        if check:
+            k = int(info.item())
+            if k > 0:
+                raise np.linalg.LinAlgError(f"{k}-th leading minor of the array is not positive definite")
+
+
+def pobtasi(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_arrow_tip_block, **kwargs):
+    """Selected inversion of a block tridiagonal with arrowhead matrix from its Cholesky factor, in place.
+
+    Mirrors src/serinv/algs/pobtasi.py:10-89.  Keyword arguments:
+    ``device_streaming`` (accepted), ``buffer`` (permuted variant: not
+    supported yet), ``invert_last_block`` (default True).  Unknown keywords
+    raise TypeError (pobtasi.py:45-48).
+    """
+    unexpected = set(kwargs) - _POBTASI_KW - _EXTENSION_KW
+    if unexpected:
+        raise TypeError(f"Unexpected keyword arguments: {unexpected}")
+    if kwargs.get("buffer", None) is not None:
+        raise NotImplementedError("the permuted (buffer=) selected inversion is not supported yet")
+    invert_last_block = bool(kwargs.get("invert_last_block", True))
+    precision = _precision(kwargs)
+
+    lib = _lib.load()
+    device, w = _prepare(
+        (L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_arrow_tip_block),
+        ("L_diagonal_blocks", "L_lower_diagonal_blocks", "L_lower_arrow_blocks", "L_arrow_tip_block"))
+    m = _bta_struct(*(x.t for x in w))
+    with torch.cuda.device(device):
+        nbytes = ctypes.c_size_t(0)
+        _lib.raise_for(lib.sgb_pobtasi_workspace_size(ctypes.byref(m), precision, ctypes.byref(nbytes)),
+                       "pobtasi")
+        ws = _workspace(nbytes.value, device)
+        rc = lib.sgb_pobtasi(ctypes.byref(m), int(invert_last_block), precision, ws.data_ptr(), nbytes.value,
+                             _stream(device))
+        _lib.raise_for(rc, "pobtasi")
+        _finish(w)
+
+
+def pobtas(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_arrow_tip_block, B, trans="N",
+           **kwargs):
+    """Triangular solve with the Cholesky factor of a BTA matrix, in place on ``B``.
+
+    Mirrors src/serinv/algs/pobtas.py:10-62: ``trans="N"`` computes
+    ``B <- L^{-1} B``, ``"T"``/``"C"`` computes ``B <- L^{-T} B``, anything
+    else raises ValueError (pobtas.py:160-161).  ``partial=True`` skips the
+    last diagonal block and the tip.  ``device_streaming`` and ``buffer``
+    raise NotImplementedError (pobtas.py:33-36,49-52; the permuted solve is
+    not supported yet).  Like the reference, unknown keywords are ignored.
+    For arrow width 0 the call is the arrow-free solve of
+    src/serinv/algs/pobts.py:57-118 (the reference's pobtas fails there).
+    """
+    if kwargs.get("device_streaming", False):
+        raise NotImplementedError("Streaming is not implemented for the natural arrowhead.")
+    if kwargs.get("buffer", None) is not None:
+        raise NotImplementedError("the permuted (buffer=) solve is not supported yet")
+    if trans not in ("N", "T", "C"):
+        raise ValueError(f"Invalid transpose argument: {trans}.")
+    partial = bool(kwargs.get("partial", False))
+    precision = _precision(kwargs)
+
+    lib = _lib.load()
+    device, w = _prepare(
+        (L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_arrow_tip_block, B),
+        ("L_diagonal_blocks", "L_lower_diagonal_blocks", "L_lower_arrow_blocks", "L_arrow_tip_block", "B"))
+    m = _bta_struct(*(x.t for x in w[:4]))
+    Bt = w[4].t
+    squeeze = Bt.dim() == 1
+    if squeeze:
+        Bt = Bt.view(-1, 1)
+    N = m.n * m.b + m.a
+    if Bt.dim() != 2 or Bt.shape[0] != N:
+        raise ValueError(f"B must have shape ({N}, nrhs), got {tuple(w[4].t.shape)}")
+    if Bt.dtype != w[0].t.dtype:
+        raise TypeError(f"B has dtype {Bt.dtype}, the factor has {w[0].t.dtype}")
+    nrhs = Bt.shape[1]
+    with torch.cuda.device(device):
+        nbytes = ctypes.c_size_t(0)
+        _lib.raise_for(lib.sgb_pobtas_workspace_size(ctypes.byref(m), nrhs, precision, ctypes.byref(nbytes)),
+                       "pobtas")
+        ws = _workspace(nbytes.value, device)
+        rc = lib.sgb_pobtas(ctypes.byref(m), _ptr(Bt), nrhs, max(nrhs, 1), trans.encode(), int(partial),
+                            precision, ws.data_ptr(), nbytes.value, _stream(device))
+        _lib.raise_for(rc, "pobtas")
+        _finish(w)

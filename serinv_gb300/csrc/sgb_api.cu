@@ -1,0 +1,582 @@
+// C ABI entry points: argument checks, workspace layout, and the host-side
+// block sweeps of pobtaf / pobtasi / pobtas that enqueue the kernels.
+#include <string.h>
+
+#include "sgb_internal.cuh"
+
+namespace sgb {
+namespace {
+
+thread_local int g_last_cuda_error = 0;
+
+int cuda_fail(cudaError_t e) {
+    g_last_cuda_error = (int)e;
+    return SGB_ERR_CUDA;
+}
+
+#define SGB_TRY(expr)                                     \
+    do {                                                  \
+        cudaError_t _e = (expr);                          \
+        if (_e != cudaSuccess) return cuda_fail(_e);      \
+    } while (0)
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+// Largest sizes the 32-bit tile indexing handles comfortably.
+constexpr int64_t kMaxBlock = 1 << 16;
+
+int check_bta(const sgb_bta* m) {
+    if (m == nullptr) return SGB_ERR_ARG;
+    if (m->dtype != SGB_F32 && m->dtype != SGB_F64) return SGB_ERR_DTYPE;
+    if (m->n < 1 || m->b < 1 || m->a < 0) return SGB_ERR_SHAPE;
+    if (m->b > kMaxBlock || m->a > kMaxBlock || m->n > (int64_t)1 << 30) return SGB_ERR_SHAPE;
+    if (m->diag == nullptr) return SGB_ERR_ARG;
+    if (m->n > 1 && m->lower == nullptr) return SGB_ERR_ARG;
+    if (m->a > 0 && (m->arrow == nullptr || m->tip == nullptr)) return SGB_ERR_ARG;
+    return SGB_OK;
+}
+
+int check_precision(int precision) {
+    if (precision == SGB_PREC_NATIVE) return SGB_OK;
+    if (precision == SGB_PREC_MIXED) return SGB_ERR_UNSUPPORTED;
+    return SGB_ERR_ARG;
+}
+
+// ---- workspace layouts ------------------------------------------------
+
+struct Carve {
+    size_t off = 0;
+    size_t take(size_t bytes) {
+        size_t o = off;
+        off = align_up(off + bytes);
+        return o;
+    }
+};
+
+template <typename T>
+struct PobtafWs {
+    size_t tinv, total;
+    PobtafWs(const sgb_bta*) {
+        Carve c;
+        tinv = c.take(sizeof(T) * kTile * kTile);
+        total = c.off;
+    }
+};
+
+template <typename T>
+struct PobtasiWs {
+    size_t linv, linv_tip, trtri, uv, xt, w, total;
+    PobtasiWs(const sgb_bta* m) {
+        const size_t n = m->n, b = m->b, a = m->a;
+        const size_t mx = b > a ? b : a;
+        Carve c;
+        linv = c.take(sizeof(T) * n * b * b);
+        linv_tip = c.take(sizeof(T) * a * a);
+        trtri = c.take(sizeof(T) * n * kTile * mx);
+        uv = c.take(sizeof(T) * (b + a) * b);
+        xt = c.take(sizeof(T) * (b + a) * b);
+        w = c.take(sizeof(T) * b * b);
+        total = c.off;
+    }
+};
+
+template <typename T>
+struct PobtasWs {
+    size_t linv, linv_tip, trtri, y, total;
+    PobtasWs(const sgb_bta* m, int64_t nrhs) {
+        const size_t n = m->n, b = m->b, a = m->a;
+        const size_t mx = b > a ? b : a;
+        Carve c;
+        linv = c.take(sizeof(T) * n * b * b);
+        linv_tip = c.take(sizeof(T) * a * a);
+        trtri = c.take(sizeof(T) * n * kTile * mx);
+        y = c.take(sizeof(T) * mx * (size_t)nrhs);
+        total = c.off;
+    }
+};
+
+int check_ws(void* ws, size_t have, size_t need) {
+    if (need == 0) return SGB_OK;
+    if (ws == nullptr || have < need) return SGB_ERR_WORKSPACE;
+    if (((uintptr_t)ws) % kAlign != 0) return SGB_ERR_WORKSPACE;
+    return SGB_OK;
+}
+
+template <typename T>
+GemmProb<T> prob() {
+    GemmProb<T> p;
+    memset(&p, 0, sizeof(p));
+    p.batch = 1;
+    p.alpha = T(1);
+    return p;
+}
+
+template <typename T>
+void set_term(GemmProb<T>& p, int t, const T* A, int64_t lda, int transA, const T* B, int64_t ldb, int transB,
+              int64_t K, int kmode = KM_FULL) {
+    p.term[t].A = A;
+    p.term[t].lda = lda;
+    p.term[t].transA = (int8_t)transA;
+    p.term[t].B = B;
+    p.term[t].ldb = ldb;
+    p.term[t].transB = (int8_t)transB;
+    p.term[t].K = (int32_t)K;
+    p.term[t].kmode = (int8_t)kmode;
+    if (t + 1 > p.nterms) p.nterms = t + 1;
+}
+
+// Copy problem: Cout = Cin (M x N).
+template <typename T>
+GemmProb<T> copy_prob(T* dst, int64_t ldd, const T* src, int64_t lds, int64_t M, int64_t N) {
+    GemmProb<T> p = prob<T>();
+    p.M = (int32_t)M;
+    p.N = (int32_t)N;
+    p.alpha = T(0);
+    p.beta = T(1);
+    p.Cin = src;
+    p.ldcin = lds;
+    p.Cout = dst;
+    p.ldc = ldd;
+    return p;
+}
+
+// ---- pobtaf -------------------------------------------------------------
+// Block Cholesky, src/serinv/algs/pobtaf.py:97-183.  Per block i:
+//   [D_i; Lo_i; Ar_i] <- blocked Cholesky of the column block  (:117-139)
+//   D_{i+1} -= Lo_i Lo_i^T, Ar_{i+1} -= Ar_i Lo_i^T, T -= Ar_i Ar_i^T  (:143-159)
+template <typename T>
+int pobtaf_native(const sgb_bta* m, int factorize_last_block, void* ws, int32_t* info, cudaStream_t s) {
+    const int64_t n = m->n, b = m->b, a = m->a;
+    T* D = (T*)m->diag;
+    T* Lo = (T*)m->lower;
+    T* Ar = (T*)m->arrow;
+    T* Tp = (T*)m->tip;
+    PobtafWs<T> L(m);
+    T* tinv = (T*)((char*)ws + L.tinv);
+    const int64_t bb = b * b, ab = a * b;
+
+    for (int64_t i = 0; i < n - 1; ++i) {
+        RowSet<T> r1{Lo + i * bb, b, b};
+        RowSet<T> r2{a ? Ar + i * ab : nullptr, a, b};
+        int rc = (int)factor_column_block<T>(D + i * bb, b, b, r1, r2, tinv, info, i * b, s);
+        if (rc != cudaSuccess) return cuda_fail((cudaError_t)rc);
+
+        const bool next_factored = (i + 1 < n - 1) || factorize_last_block;
+        GemmProb<T> pr[3];
+        int np = 0;
+        {   // D_{i+1} -= Lo_i Lo_i^T
+            GemmProb<T> p = prob<T>();
+            p.M = p.N = (int32_t)b;
+            set_term<T>(p, 0, Lo + i * bb, b, 0, Lo + i * bb, b, 1, b);
+            p.alpha = T(-1);
+            p.beta = T(1);
+            p.Cin = p.Cout = D + (i + 1) * bb;
+            p.ldcin = p.ldc = b;
+            p.lower_only = next_factored ? 1 : 0;
+            pr[np++] = p;
+        }
+        if (a) {
+            GemmProb<T> p = prob<T>();  // Ar_{i+1} -= Ar_i Lo_i^T
+            p.M = (int32_t)a;
+            p.N = (int32_t)b;
+            set_term<T>(p, 0, Ar + i * ab, b, 0, Lo + i * bb, b, 1, b);
+            p.alpha = T(-1);
+            p.beta = T(1);
+            p.Cin = p.Cout = Ar + (i + 1) * ab;
+            p.ldcin = p.ldc = b;
+            pr[np++] = p;
+            GemmProb<T> q = prob<T>();  // T -= Ar_i Ar_i^T
+            q.M = q.N = (int32_t)a;
+            set_term<T>(q, 0, Ar + i * ab, b, 0, Ar + i * ab, b, 1, b);
+            q.alpha = T(-1);
+            q.beta = T(1);
+            q.Cin = q.Cout = Tp;
+            q.ldcin = q.ldc = a;
+            q.lower_only = factorize_last_block ? 1 : 0;
+            pr[np++] = q;
+        }
+        SGB_TRY(gemm_simt<T>(pr, np, s));
+    }
+
+    if (factorize_last_block) {
+        const int64_t i = n - 1;
+        RowSet<T> r1{nullptr, 0, b};
+        RowSet<T> r2{a ? Ar + i * ab : nullptr, a, b};
+        int rc = (int)factor_column_block<T>(D + i * bb, b, b, r1, r2, tinv, info, i * b, s);
+        if (rc != cudaSuccess) return cuda_fail((cudaError_t)rc);
+        if (a) {
+            GemmProb<T> q = prob<T>();  // T -= Ar_{n-1} Ar_{n-1}^T  (:177-180)
+            q.M = q.N = (int32_t)a;
+            set_term<T>(q, 0, Ar + i * ab, b, 0, Ar + i * ab, b, 1, b);
+            q.alpha = T(-1);
+            q.beta = T(1);
+            q.Cin = q.Cout = Tp;
+            q.ldcin = q.ldc = a;
+            q.lower_only = 1;
+            SGB_TRY(gemm_simt<T>(&q, 1, s));
+            RowSet<T> none{nullptr, 0, a};
+            rc = (int)factor_column_block<T>(Tp, a, a, none, none, tinv, info, n * b, s);  // :183
+            if (rc != cudaSuccess) return cuda_fail((cudaError_t)rc);
+        }
+    }
+    return SGB_OK;
+}
+
+// ---- pobtasi ------------------------------------------------------------
+// Selected inversion, src/serinv/algs/pobtasi.py:92-172.  All L_ii^{-1} are
+// independent of the back-sweep, so they are formed up front in one batched
+// triangular inversion.  Per block i (from the last one):
+//   U = -X_D[i+1] Lo_i - X_A[i+1]^T Ar_i ;  V = -X_A[i+1] Lo_i - X_T Ar_i    (:153-163)
+//   X_Lo = U L_ii^{-1} ; X_A = V L_ii^{-1}
+//   X_D  = (L_ii^{-T} - X_Lo^T Lo_i - X_A^T Ar_i) L_ii^{-1}                  (:167-172)
+// The last block (:114-139) is the same step without the i+1 terms.
+template <typename T>
+int pobtasi_native(const sgb_bta* m, int invert_last_block, void* ws, cudaStream_t s) {
+    const int64_t n = m->n, b = m->b, a = m->a;
+    T* D = (T*)m->diag;
+    T* Lo = (T*)m->lower;
+    T* Ar = (T*)m->arrow;
+    T* Tp = (T*)m->tip;
+    PobtasiWs<T> W(m);
+    char* base = (char*)ws;
+    T* Linv = (T*)(base + W.linv);
+    T* Ltinv = (T*)(base + W.linv_tip);
+    T* trs = (T*)(base + W.trtri);
+    T* UV = (T*)(base + W.uv);
+    T* XT = (T*)(base + W.xt);
+    T* Wm = (T*)(base + W.w);
+    const int64_t bb = b * b, ab = a * b;
+
+    const int64_t ninv = invert_last_block ? n : n - 1;
+    SGB_TRY(trtri_batched<T>(D, b, bb, b, ninv, Linv, b, bb, trs, s));
+
+    if (invert_last_block && a) {
+        // X_T = L_T^{-T} L_T^{-1}  (:115-119)
+        SGB_TRY(trtri_batched<T>(Tp, a, a * a, a, 1, Ltinv, a, a * a, trs, s));
+        GemmProb<T> p = prob<T>();
+        p.M = p.N = (int32_t)a;
+        set_term<T>(p, 0, Ltinv, a, 1, Ltinv, a, 0, a, KM_GE_M0);
+        p.Cout = Tp;
+        p.ldc = a;
+        SGB_TRY(gemm_simt<T>(&p, 1, s));
+    }
+
+    const int64_t first = invert_last_block ? n - 1 : n - 2;
+    for (int64_t i = first; i >= 0; --i) {
+        const bool has_next = i < n - 1;
+        const T* Li = Linv + i * bb;
+        T* Di = D + i * bb;
+        T* Loi = has_next ? Lo + i * bb : nullptr;
+        T* Ari = a ? Ar + i * ab : nullptr;
+        T* U = UV;
+        T* V = UV + bb;
+        T* XLo = XT;
+        T* XA = XT + bb;
+
+        // (1) U, V
+        GemmProb<T> pr[3];
+        int np = 0;
+        if (has_next) {
+            GemmProb<T> p = prob<T>();
+            p.M = p.N = (int32_t)b;
+            set_term<T>(p, 0, D + (i + 1) * bb, b, 0, Loi, b, 0, b);
+            if (a) set_term<T>(p, 1, Ar + (i + 1) * ab, b, 1, Ari, b, 0, a);
+            p.alpha = T(-1);
+            p.Cout = U;
+            p.ldc = b;
+            pr[np++] = p;
+        }
+        if (a) {
+            GemmProb<T> p = prob<T>();
+            p.M = (int32_t)a;
+            p.N = (int32_t)b;
+            int t = 0;
+            if (has_next) set_term<T>(p, t++, Ar + (i + 1) * ab, b, 0, Loi, b, 0, b);
+            set_term<T>(p, t, Tp, a, 0, Ari, b, 0, a);
+            p.alpha = T(-1);
+            p.Cout = V;
+            p.ldc = b;
+            pr[np++] = p;
+        }
+        if (np) SGB_TRY(gemm_simt<T>(pr, np, s));
+
+        // (2) X_Lo = U Linv, X_A = V Linv
+        np = 0;
+        if (has_next) {
+            GemmProb<T> p = prob<T>();
+            p.M = p.N = (int32_t)b;
+            set_term<T>(p, 0, U, b, 0, Li, b, 0, b, KM_GE_N0);
+            p.Cout = XLo;
+            p.ldc = b;
+            pr[np++] = p;
+        }
+        if (a) {
+            GemmProb<T> p = prob<T>();
+            p.M = (int32_t)a;
+            p.N = (int32_t)b;
+            set_term<T>(p, 0, V, b, 0, Li, b, 0, b, KM_GE_N0);
+            p.Cout = XA;
+            p.ldc = b;
+            pr[np++] = p;
+        }
+        if (np) SGB_TRY(gemm_simt<T>(pr, np, s));
+
+        // (3) W = Linv^T - X_Lo^T Lo_i - X_A^T Ar_i
+        {
+            GemmProb<T> p = prob<T>();
+            p.M = p.N = (int32_t)b;
+            int t = 0;
+            if (has_next) set_term<T>(p, t++, XLo, b, 1, Loi, b, 0, b);
+            if (a) set_term<T>(p, t++, XA, b, 1, Ari, b, 0, a);
+            p.alpha = T(-1);
+            p.beta = T(1);
+            p.Cin = Li;
+            p.ldcin = b;
+            p.transCin = 1;
+            p.Cout = Wm;
+            p.ldc = b;
+            SGB_TRY(gemm_simt<T>(&p, 1, s));
+        }
+
+        // (4) X_D = W Linv ; Lo_i <- X_Lo ; Ar_i <- X_A
+        np = 0;
+        {
+            GemmProb<T> p = prob<T>();
+            p.M = p.N = (int32_t)b;
+            set_term<T>(p, 0, Wm, b, 0, Li, b, 0, b, KM_GE_N0);
+            p.Cout = Di;
+            p.ldc = b;
+            pr[np++] = p;
+        }
+        if (has_next) pr[np++] = copy_prob<T>(Loi, b, XLo, b, b, b);
+        if (a) pr[np++] = copy_prob<T>(Ari, b, XA, b, a, b);
+        SGB_TRY(gemm_simt<T>(pr, np, s));
+    }
+    return SGB_OK;
+}
+
+// ---- pobtas -------------------------------------------------------------
+// Block triangular solve, src/serinv/algs/pobtas.py:65-161.  The diagonal
+// solves use L_ii^{-1} (one batched triangular inversion up front), so every
+// block step is two grouped products.
+template <typename T>
+int pobtas_native(const sgb_bta* m, T* Bm, int64_t nrhs, int64_t ldb, char trans, int partial, void* ws,
+                  cudaStream_t s) {
+    const int64_t n = m->n, b = m->b, a = m->a;
+    T* D = (T*)m->diag;
+    T* Lo = (T*)m->lower;
+    T* Ar = (T*)m->arrow;
+    T* Tp = (T*)m->tip;
+    PobtasWs<T> W(m, nrhs);
+    char* base = (char*)ws;
+    T* Linv = (T*)(base + W.linv);
+    T* Ltinv = (T*)(base + W.linv_tip);
+    T* trs = (T*)(base + W.trtri);
+    T* y = (T*)(base + W.y);
+    const int64_t bb = b * b, ab = a * b;
+    T* Btip = Bm + n * b * ldb;
+    auto Bi = [&](int64_t i) { return Bm + i * b * ldb; };
+
+    if (nrhs == 0) return SGB_OK;
+    SGB_TRY(trtri_batched<T>(D, b, bb, b, n, Linv, b, bb, trs, s));
+    if (a && !partial) SGB_TRY(trtri_batched<T>(Tp, a, a * a, a, 1, Ltinv, a, a * a, trs, s));
+
+    if (trans == 'N') {
+        const int64_t last = partial ? n - 1 : n;
+        for (int64_t i = 0; i < last; ++i) {
+            // y = L_ii^{-1} B_i
+            GemmProb<T> p = prob<T>();
+            p.M = (int32_t)b;
+            p.N = (int32_t)nrhs;
+            set_term<T>(p, 0, Linv + i * bb, b, 0, Bi(i), ldb, 0, b, KM_LT_M1);
+            p.Cout = y;
+            p.ldc = nrhs;
+            SGB_TRY(gemm_simt<T>(&p, 1, s));
+            // B_i = y ; B_{i+1} -= Lo_i y ; B_tip -= Ar_i y
+            GemmProb<T> pr[3];
+            int np = 0;
+            pr[np++] = copy_prob<T>(Bi(i), ldb, y, nrhs, b, nrhs);
+            if (i < n - 1) {
+                GemmProb<T> q = prob<T>();
+                q.M = (int32_t)b;
+                q.N = (int32_t)nrhs;
+                set_term<T>(q, 0, Lo + i * bb, b, 0, y, nrhs, 0, b);
+                q.alpha = T(-1);
+                q.beta = T(1);
+                q.Cin = q.Cout = Bi(i + 1);
+                q.ldcin = q.ldc = ldb;
+                pr[np++] = q;
+            }
+            if (a) {
+                GemmProb<T> q = prob<T>();
+                q.M = (int32_t)a;
+                q.N = (int32_t)nrhs;
+                set_term<T>(q, 0, Ar + i * ab, b, 0, y, nrhs, 0, b);
+                q.alpha = T(-1);
+                q.beta = T(1);
+                q.Cin = q.Cout = Btip;
+                q.ldcin = q.ldc = ldb;
+                pr[np++] = q;
+            }
+            SGB_TRY(gemm_simt<T>(pr, np, s));
+        }
+        if (!partial && a) {
+            // B_tip = L_T^{-1} B_tip  (:124-126)
+            GemmProb<T> p = prob<T>();
+            p.M = (int32_t)a;
+            p.N = (int32_t)nrhs;
+            set_term<T>(p, 0, Ltinv, a, 0, Btip, ldb, 0, a, KM_LT_M1);
+            p.Cout = y;
+            p.ldc = nrhs;
+            SGB_TRY(gemm_simt<T>(&p, 1, s));
+            GemmProb<T> c = copy_prob<T>(Btip, ldb, y, nrhs, a, nrhs);
+            SGB_TRY(gemm_simt<T>(&c, 1, s));
+        }
+        return SGB_OK;
+    }
+
+    // trans 'T' / 'C' (real arithmetic: identical)
+    if (!partial) {
+        if (a) {
+            // B_tip = L_T^{-T} B_tip  (:131-136)
+            GemmProb<T> p = prob<T>();
+            p.M = (int32_t)a;
+            p.N = (int32_t)nrhs;
+            set_term<T>(p, 0, Ltinv, a, 1, Btip, ldb, 0, a, KM_GE_M0);
+            p.Cout = y;
+            p.ldc = nrhs;
+            SGB_TRY(gemm_simt<T>(&p, 1, s));
+            GemmProb<T> c = copy_prob<T>(Btip, ldb, y, nrhs, a, nrhs);
+            SGB_TRY(gemm_simt<T>(&c, 1, s));
+        }
+    }
+    const int64_t first = partial ? n - 2 : n - 1;
+    for (int64_t i = first; i >= 0; --i) {
+        // B_i -= Lo_i^T B_{i+1} + Ar_i^T B_tip  (:139-159)
+        GemmProb<T> p = prob<T>();
+        p.M = (int32_t)b;
+        p.N = (int32_t)nrhs;
+        int t = 0;
+        if (i < n - 1) set_term<T>(p, t++, Lo + i * bb, b, 1, Bi(i + 1), ldb, 0, b);
+        if (a) set_term<T>(p, t++, Ar + i * ab, b, 1, Btip, ldb, 0, a);
+        if (t) {
+            p.alpha = T(-1);
+            p.beta = T(1);
+            p.Cin = p.Cout = Bi(i);
+            p.ldcin = p.ldc = ldb;
+            SGB_TRY(gemm_simt<T>(&p, 1, s));
+        }
+        // B_i = L_ii^{-T} B_i
+        GemmProb<T> q = prob<T>();
+        q.M = (int32_t)b;
+        q.N = (int32_t)nrhs;
+        set_term<T>(q, 0, Linv + i * bb, b, 1, Bi(i), ldb, 0, b, KM_GE_M0);
+        q.Cout = y;
+        q.ldc = nrhs;
+        SGB_TRY(gemm_simt<T>(&q, 1, s));
+        GemmProb<T> c = copy_prob<T>(Bi(i), ldb, y, nrhs, b, nrhs);
+        SGB_TRY(gemm_simt<T>(&c, 1, s));
+    }
+    return SGB_OK;
+}
+
+}  // namespace
+}  // namespace sgb
+
+using namespace sgb;
+
+extern "C" {
+
+int sgb_version(void) { return 100; }
+
+const char* sgb_strerror(int code) {
+    switch (code) {
+        case SGB_OK: return "ok";
+        case SGB_ERR_SHAPE: return "invalid shape";
+        case SGB_ERR_DTYPE: return "unsupported dtype";
+        case SGB_ERR_NOT_SPD: return "matrix is not positive definite";
+        case SGB_ERR_TIMEOUT: return "device wait timed out";
+        case SGB_ERR_CUDA: return "CUDA runtime error";
+        case SGB_ERR_WORKSPACE: return "workspace missing, too small or misaligned";
+        case SGB_ERR_ARG: return "invalid argument";
+        case SGB_ERR_UNSUPPORTED: return "not supported by this build";
+        default: return "unknown error";
+    }
+}
+
+int sgb_last_cuda_error(void) { return g_last_cuda_error; }
+
+int sgb_pobtaf_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    if ((rc = check_precision(precision))) return rc;
+    if (!bytes) return SGB_ERR_ARG;
+    *bytes = m->dtype == SGB_F64 ? PobtafWs<double>(m).total : PobtafWs<float>(m).total;
+    return SGB_OK;
+}
+
+int sgb_pobtasi_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    if ((rc = check_precision(precision))) return rc;
+    if (!bytes) return SGB_ERR_ARG;
+    *bytes = m->dtype == SGB_F64 ? PobtasiWs<double>(m).total : PobtasiWs<float>(m).total;
+    return SGB_OK;
+}
+
+int sgb_pobtas_workspace_size(const sgb_bta* m, int64_t nrhs, int precision, size_t* bytes) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    if ((rc = check_precision(precision))) return rc;
+    if (!bytes) return SGB_ERR_ARG;
+    if (nrhs < 0 || nrhs > (1 << 20)) return SGB_ERR_SHAPE;
+    *bytes = m->dtype == SGB_F64 ? PobtasWs<double>(m, nrhs).total : PobtasWs<float>(m, nrhs).total;
+    return SGB_OK;
+}
+
+int sgb_pobtaf(const sgb_bta* m, int factorize_last_block, int precision, void* workspace,
+               size_t workspace_bytes, int32_t* info, void* stream) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    if ((rc = check_precision(precision))) return rc;
+    size_t need = 0;
+    sgb_pobtaf_workspace_size(m, precision, &need);
+    if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
+    if (m->dtype == SGB_F64) return pobtaf_native<double>(m, factorize_last_block, workspace, info, s);
+    return pobtaf_native<float>(m, factorize_last_block, workspace, info, s);
+}
+
+int sgb_pobtasi(const sgb_bta* m, int invert_last_block, int precision, void* workspace, size_t workspace_bytes,
+                void* stream) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    if ((rc = check_precision(precision))) return rc;
+    size_t need = 0;
+    sgb_pobtasi_workspace_size(m, precision, &need);
+    if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (m->dtype == SGB_F64) return pobtasi_native<double>(m, invert_last_block, workspace, s);
+    return pobtasi_native<float>(m, invert_last_block, workspace, s);
+}
+
+int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char trans, int partial, int precision,
+               void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    if ((rc = check_precision(precision))) return rc;
+    if (trans != 'N' && trans != 'T' && trans != 'C') return SGB_ERR_ARG;
+    if (nrhs < 0 || nrhs > (1 << 20) || ldb < nrhs) return SGB_ERR_SHAPE;
+    if (nrhs > 0 && rhs == nullptr) return SGB_ERR_ARG;
+    size_t need = 0;
+    sgb_pobtas_workspace_size(m, nrhs, precision, &need);
+    if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (m->dtype == SGB_F64)
+        return pobtas_native<double>(m, (double*)rhs, nrhs, ldb, trans, partial, workspace, s);
+    return pobtas_native<float>(m, (float*)rhs, nrhs, ldb, trans, partial, workspace, s);
+}
+
+}  // extern "C"

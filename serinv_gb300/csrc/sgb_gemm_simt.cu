@@ -1,0 +1,195 @@
+// Grouped, batched SIMT GEMM in the storage precision (FP64 DFMA / FP32 FFMA).
+//
+// One launch processes up to kMaxProbs independent problems
+//   Cout = alpha * sum_t op(A_t) op(B_t) + beta * op(Cin)
+// each optionally batched.  Every CTA computes one 32 x 32 output tile.
+// The tile is small on purpose: on GB300 the FP64 pipe retires about two
+// DFMA per SM per clock, so a 32 x 32 x 512 tile already runs for ~100 us
+// and small tiles are what spreads the block-step GEMMs (512 x 512) over
+// all 152 SMs.  Operand tiles are staged through shared memory with
+// coalesced loads for either storage orientation.
+#include "sgb_internal.cuh"
+
+namespace sgb {
+
+namespace {
+
+constexpr int BM = 32, BN = 32, BK = 16, NT = 256;
+constexpr int TM = 2, TN = 2;  // rows ty + 16*i, cols tx + 16*j
+
+template <typename T>
+__device__ __forceinline__ void k_range(const GemmTerm<T>& t, int m0, int n0, int& klo, int& khi) {
+    klo = 0;
+    khi = t.K;
+    switch (t.kmode) {
+        case KM_GE_N0: klo = n0; break;
+        case KM_LT_N1: khi = min(t.K, n0 + BN); break;
+        case KM_GE_M0: klo = m0; break;
+        case KM_LT_M1: khi = min(t.K, m0 + BM); break;
+        default: break;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_gemm_simt(const __grid_constant__ GemmLaunch<T> L) {
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN + 1];
+
+    const int tile = blockIdx.x;
+    int pi = 0;
+#pragma unroll 1
+    for (int q = 1; q < L.np; ++q)
+        if (tile >= L.p[q].tile_begin) pi = q;
+    const GemmProb<T>& P = L.p[pi];
+
+    int local = tile - P.tile_begin;
+    const int per_inst = P.tiles_m * P.tiles_n;
+    const int inst = local / per_inst;
+    local -= inst * per_inst;
+    const int tm = local / P.tiles_n;
+    const int tn = local - tm * P.tiles_n;
+    const int m0 = tm * BM, n0 = tn * BN;
+    if (P.lower_only && n0 >= m0 + BM) return;  // strictly above the diagonal
+
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+
+    T acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+
+#pragma unroll 1
+    for (int ti = 0; ti < P.nterms; ++ti) {
+        const GemmTerm<T>& t = P.term[ti];
+        const T* A = t.A + (int64_t)inst * t.strideA;
+        const T* B = t.B + (int64_t)inst * t.strideB;
+        int klo, khi;
+        k_range(t, m0, n0, klo, khi);
+#pragma unroll 1
+        for (int k0 = klo; k0 < khi; k0 += BK) {
+            // A tile: op(A)[m0 .. m0+BM) x [k0 .. k0+BK)
+#pragma unroll
+            for (int e = tid; e < BM * BK; e += NT) {
+                int m, k;
+                if (t.transA) { m = e % BM; k = e / BM; }
+                else          { k = e % BK; m = e / BK; }
+                const int gm = m0 + m, gk = k0 + k;
+                T v = T(0);
+                if (gm < P.M && gk < khi)
+                    v = t.transA ? A[(int64_t)gk * t.lda + gm] : A[(int64_t)gm * t.lda + gk];
+                As[k][m] = v;
+            }
+            // B tile: op(B)[k0 .. k0+BK) x [n0 .. n0+BN)
+#pragma unroll
+            for (int e = tid; e < BK * BN; e += NT) {
+                int n, k;
+                if (t.transB) { k = e % BK; n = e / BK; }
+                else          { n = e % BN; k = e / BN; }
+                const int gn = n0 + n, gk = k0 + k;
+                T v = T(0);
+                if (gn < P.N && gk < khi)
+                    v = t.transB ? B[(int64_t)gn * t.ldb + gk] : B[(int64_t)gk * t.ldb + gn];
+                Bs[k][n] = v;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int kk = 0; kk < BK; ++kk) {
+                T a[TM], bb[TN];
+#pragma unroll
+                for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+                for (int j = 0; j < TN; ++j) bb[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+                for (int i = 0; i < TM; ++i)
+#pragma unroll
+                    for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+            }
+            __syncthreads();
+        }
+    }
+
+    T* C = P.Cout + (int64_t)inst * P.strideC;
+    const T* Ci = P.Cin ? P.Cin + (int64_t)inst * P.strideCin : nullptr;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        const int gm = m0 + ty + 16 * i;
+        if (gm >= P.M) continue;
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const int gn = n0 + tx + 16 * j;
+            if (gn >= P.N) continue;
+            T v = P.alpha * acc[i][j];
+            if (Ci != nullptr && P.beta != T(0)) {
+                const T c = P.transCin ? Ci[(int64_t)gn * P.ldcin + gm] : Ci[(int64_t)gm * P.ldcin + gn];
+                v = fma(P.beta, c, v);
+            }
+            C[(int64_t)gm * P.ldc + gn] = v;
+        }
+    }
+}
+
+}  // namespace
+
+template <typename T>
+double useful_flops(const GemmProb<T>& p) {
+    // 2 * sum over output elements of the K-range each term needs.
+    double f = 0.0;
+    for (int t = 0; t < p.nterms; ++t) {
+        const GemmTerm<T>& tm = p.term[t];
+        const int64_t K = tm.K;
+        double s = 0.0;
+        if (tm.kmode == KM_GE_M0 || tm.kmode == KM_LT_M1) {
+            for (int64_t m = 0; m < p.M; ++m) {
+                const int64_t kl = tm.kmode == KM_GE_M0 ? (K - m > 0 ? K - m : 0) : (m + 1 < K ? m + 1 : K);
+                const int64_t ncols = p.lower_only ? (m + 1 < p.N ? m + 1 : p.N) : p.N;
+                s += (double)kl * ncols;
+            }
+        } else {
+            for (int64_t n = 0; n < p.N; ++n) {
+                int64_t kl = K;
+                if (tm.kmode == KM_GE_N0) kl = K - n > 0 ? K - n : 0;
+                if (tm.kmode == KM_LT_N1) kl = n + 1 < K ? n + 1 : K;
+                const int64_t nrows = p.lower_only ? (p.M - n > 0 ? p.M - n : 0) : p.M;
+                s += (double)kl * nrows;
+            }
+        }
+        f += 2.0 * s;
+    }
+    return f * p.batch;
+}
+
+template double useful_flops<double>(const GemmProb<double>&);
+template double useful_flops<float>(const GemmProb<float>&);
+
+template <typename T>
+cudaError_t gemm_simt(GemmProb<T>* probs, int np, cudaStream_t s) {
+    GemmLaunch<T> L;
+    L.np = 0;
+    int64_t total = 0;
+    for (int i = 0; i < np; ++i) {
+        GemmProb<T> p = probs[i];
+        if (p.M <= 0 || p.N <= 0 || p.batch <= 0) continue;
+        p.tiles_m = (int32_t)ceil_div(p.M, BM);
+        p.tiles_n = (int32_t)ceil_div(p.N, BN);
+        p.tile_begin = (int32_t)total;
+        total += (int64_t)p.tiles_m * p.tiles_n * p.batch;
+        L.p[L.np++] = p;
+        if (L.np == kMaxProbs && i + 1 < np) return cudaErrorInvalidValue;
+    }
+    if (L.np == 0) return cudaSuccess;
+    if (total > 0x7fffffff) return cudaErrorInvalidValue;
+    L.total_tiles = (int32_t)total;
+    double fl = 0.0;
+    for (int i = 0; i < L.np; ++i) fl += useful_flops<T>(L.p[i]);
+    prof_before(s);
+    k_gemm_simt<T><<<(unsigned)total, NT, 0, s>>>(L);
+    prof_after(SGB_KCLASS_GEMM, s, fl);
+    return cudaGetLastError();
+}
+
+template cudaError_t gemm_simt<double>(GemmProb<double>*, int, cudaStream_t);
+template cudaError_t gemm_simt<float>(GemmProb<float>*, int, cudaStream_t);
+
+}  // namespace sgb

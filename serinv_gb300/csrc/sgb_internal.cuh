@@ -1,0 +1,113 @@
+// Internal types shared by the translation units of libserinv_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/serinv_gb300.h"
+
+namespace sgb {
+
+// Diagonal tile width of the blocked Cholesky / triangular inverse.
+constexpr int kTile = 32;
+
+// K-range restriction of one product term, for triangular operands.  The
+// stored operand must hold exact zeros where the triangle is empty; the
+// restriction only skips work.
+enum KMode : int8_t {
+    KM_FULL = 0,   // k in [0, K)
+    KM_GE_N0 = 1,  // op(B) lower triangular: k >= first column of the tile
+    KM_LT_N1 = 2,  // op(B) upper triangular: k <  last column of the tile + 1
+    KM_GE_M0 = 3,  // op(A) upper triangular: k >= first row of the tile
+    KM_LT_M1 = 4,  // op(A) lower triangular: k <  last row of the tile + 1
+};
+
+// One product term op(A) * op(B), op(A) is M x K, op(B) is K x N.  A and B
+// are row-major with leading dimensions lda / ldb; trans means the stored
+// matrix is the transpose of the operand.
+template <typename T>
+struct GemmTerm {
+    const T* A;
+    const T* B;
+    int64_t lda, ldb;
+    int64_t strideA, strideB;  // element stride between batch instances
+    int32_t K;
+    int8_t transA, transB, kmode, _pad;
+};
+
+// Cout = alpha * sum_t op(A_t) op(B_t) + beta * op(Cin), over `batch`
+// instances.  Cin may alias Cout when transCin == 0 (each element is read
+// and written by the same thread).  A term operand may alias Cout only when
+// N <= the tile width (one tile column, rows owned by one CTA).
+template <typename T>
+struct GemmProb {
+    GemmTerm<T> term[2];
+    const T* Cin;
+    T* Cout;
+    int64_t ldcin, ldc;
+    int64_t strideCin, strideC;
+    T alpha, beta;
+    int32_t M, N;
+    int32_t nterms;
+    int32_t batch;
+    int8_t lower_only;  // skip tiles strictly above the diagonal
+    int8_t transCin;
+    int8_t _pad[2];
+    // filled in by the launcher
+    int32_t tiles_m, tiles_n, tile_begin;
+};
+
+constexpr int kMaxProbs = 6;
+
+template <typename T>
+struct GemmLaunch {
+    GemmProb<T> p[kMaxProbs];
+    int32_t np;
+    int32_t total_tiles;
+};
+
+// Launch a grouped GEMM (SIMT, arithmetic in T).  Problems with M, N or
+// batch of zero are dropped.  Returns cudaSuccess or the launch error.
+template <typename T>
+cudaError_t gemm_simt(GemmProb<T>* probs, int np, cudaStream_t s);
+
+// Useful flops of one problem (2 x multiply-adds inside the triangles).
+template <typename T>
+double useful_flops(const GemmProb<T>& p);
+
+// Tile kernels (sgb_potrf.cu).
+template <typename T>
+cudaError_t potrf_tile(T* tile, int64_t ld, int nb, int zero_cols_right, T* tinv,
+                       int32_t* info, int64_t info_row0, cudaStream_t s);
+
+template <typename T>
+cudaError_t trtri_tiles_batched(const T* L, int64_t ldl, int64_t strideL, int m, int batch,
+                                T* Linv, int64_t ldx, int64_t strideX, cudaStream_t s);
+
+// Blocked in-place Cholesky of the column block [diag; rows_1; ...; rows_k]
+// (the diagonal block m x m and up to two row sets with m columns), i.e.
+// diag <- chol(diag), rows_j <- rows_j * L^{-T}.  Scratch: kTile*kTile T.
+template <typename T>
+struct RowSet {
+    T* p;
+    int64_t rows, ld;
+};
+
+template <typename T>
+cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, RowSet<T> r2,
+                                T* scratch, int32_t* info, int64_t info_row0, cudaStream_t s);
+
+// Full triangular inverse of `batch` lower-triangular m x m blocks:
+// Linv_j = L_j^{-1} (zeros above the diagonal).  Scratch: batch*kTile*m T.
+template <typename T>
+cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, int64_t batch,
+                          T* Linv, int64_t ldx, int64_t strideX, T* scratch, cudaStream_t s);
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Launch accounting (sgb_prof.cu): call prof_before just before and
+// prof_after just after every kernel launch.
+void prof_before(cudaStream_t s);
+void prof_after(int kclass, cudaStream_t s, double flops);
+
+}  // namespace sgb

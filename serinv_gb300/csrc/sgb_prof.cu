@@ -1,0 +1,105 @@
+// Launch accounting and optional per-kernel-class timing.
+//
+// Every kernel launch of the library goes through prof_before/prof_after.
+// A global counter always counts launches.  When timing is enabled,
+// CUDA events are recorded on the launching stream around each launch and
+// the algorithmic flop count of the launch is stored with them, so a caller
+// (the benchmark) can read per-class device time and achieved throughput
+// without an external profiler.
+#include <atomic>
+#include <mutex>
+#include <vector>
+
+#include "sgb_internal.cuh"
+
+namespace sgb {
+
+namespace {
+
+struct Rec {
+    int kclass;
+    cudaEvent_t a, b;
+    double flops;
+};
+
+std::atomic<long long> g_launches{0};
+std::atomic<int> g_enabled{0};
+std::mutex g_mu;
+std::vector<Rec> g_recs;
+std::vector<cudaEvent_t> g_pool;
+thread_local cudaEvent_t t_start = nullptr;
+
+cudaEvent_t get_event() {
+    if (!g_pool.empty()) {
+        cudaEvent_t e = g_pool.back();
+        g_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void recycle_locked() {
+    for (auto& r : g_recs) {
+        g_pool.push_back(r.a);
+        g_pool.push_back(r.b);
+    }
+    g_recs.clear();
+}
+
+}  // namespace
+
+void prof_before(cudaStream_t s) {
+    if (!g_enabled.load(std::memory_order_relaxed)) return;
+    std::lock_guard<std::mutex> lk(g_mu);
+    t_start = get_event();
+    cudaEventRecord(t_start, s);
+}
+
+void prof_after(int kclass, cudaStream_t s, double flops) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (!g_enabled.load(std::memory_order_relaxed) || t_start == nullptr) return;
+    std::lock_guard<std::mutex> lk(g_mu);
+    cudaEvent_t e = get_event();
+    cudaEventRecord(e, s);
+    g_recs.push_back(Rec{kclass, t_start, e, flops});
+    t_start = nullptr;
+}
+
+}  // namespace sgb
+
+using namespace sgb;
+
+extern "C" {
+
+long long sgb_launch_count(void) { return g_launches.load(); }
+
+int sgb_profile_enable(int on) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    recycle_locked();
+    g_enabled.store(on ? 1 : 0);
+    return SGB_OK;
+}
+
+int sgb_profile_read(int kclass, long long* launches, double* ms, double* flops) {
+    if (kclass < 0 || kclass >= SGB_KCLASS_COUNT || !launches || !ms || !flops) return SGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_mu);
+    long long n = 0;
+    double t = 0.0, f = 0.0;
+    for (auto& r : g_recs) {
+        if (r.kclass != kclass) continue;
+        if (cudaEventSynchronize(r.b) != cudaSuccess) return SGB_ERR_CUDA;
+        float x = 0.f;
+        if (cudaEventElapsedTime(&x, r.a, r.b) != cudaSuccess) return SGB_ERR_CUDA;
+        ++n;
+        t += x;
+        f += r.flops;
+    }
+    *launches = n;
+    *ms = t;
+    *flops = f;
+    return SGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,103 @@
+"""CPU: the C-ABI library builds, loads, exports every declared symbol, and
+rejects bad arguments on the host (no GPU call is made by these checks)."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from serinv_gb300 import _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "serinv_gb300.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(sgb_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("sgb_pobtaf", "sgb_pobtasi", "sgb_pobtas"):
+        assert s in syms
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for s in declared_symbols():
+        assert hasattr(lib, s), s
+        assert s in _lib.exported_symbols(), f"{s} has no ctypes signature"
+
+
+def test_version_and_strerror(lib):
+    assert lib.sgb_version() >= 100
+    for code in range(0, 9):
+        assert len(lib.sgb_strerror(code)) > 0
+
+
+def _desc(n=4, b=8, a=2, dtype=_lib.SGB_F64):
+    m = _lib.SgbBta()
+    m.dtype = dtype
+    m.n, m.b, m.a = n, b, a
+    # dummy non-null pointers: never dereferenced by the host-side checks
+    m.diag = m.lower = m.arrow = m.tip = 0x1000
+    return m
+
+
+def test_workspace_queries(lib):
+    m = _desc(n=4, b=64, a=16)
+    sz = ctypes.c_size_t(0)
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(m), 0, ctypes.byref(sz)) == 0
+    assert sz.value >= 32 * 32 * 8
+    assert lib.sgb_pobtasi_workspace_size(ctypes.byref(m), 0, ctypes.byref(sz)) == 0
+    assert sz.value >= 4 * 64 * 64 * 8
+    assert lib.sgb_pobtas_workspace_size(ctypes.byref(m), 16, 0, ctypes.byref(sz)) == 0
+    assert sz.value % 256 == 0
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("dtype", 7, _lib.SGB_ERR_DTYPE),
+    ("n", 0, _lib.SGB_ERR_SHAPE),
+    ("b", 0, _lib.SGB_ERR_SHAPE),
+    ("a", -1, _lib.SGB_ERR_SHAPE),
+    ("diag", 0, _lib.SGB_ERR_ARG),
+])
+def test_bad_descriptor_rejected(lib, field, value, code):
+    m = _desc()
+    setattr(m, field, value)
+    sz = ctypes.c_size_t(0)
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(m), 0, ctypes.byref(sz)) == code
+    assert lib.sgb_pobtaf(ctypes.byref(m), 1, 0, None, 0, None, None) == code
+
+
+def test_null_and_workspace_errors(lib):
+    assert lib.sgb_pobtaf(None, 1, 0, None, 0, None, None) == _lib.SGB_ERR_ARG
+    m = _desc()
+    # workspace missing / too small / misaligned: rejected before any launch
+    assert lib.sgb_pobtaf(ctypes.byref(m), 1, 0, None, 0, None, None) == _lib.SGB_ERR_WORKSPACE
+    assert lib.sgb_pobtasi(ctypes.byref(m), 1, 0, 0x1000, 8, None) == _lib.SGB_ERR_WORKSPACE
+    assert lib.sgb_pobtas(ctypes.byref(m), 0x1000, 2, 2, b"N", 0, 0, 0x1001, 1 << 30, None) == \
+        _lib.SGB_ERR_WORKSPACE
+    assert lib.sgb_pobtas(ctypes.byref(m), 0x1000, 2, 2, b"X", 0, 0, 0x1000, 1 << 30, None) == _lib.SGB_ERR_ARG
+    assert lib.sgb_pobtas(ctypes.byref(m), 0x1000, 2, 1, b"N", 0, 0, 0x1000, 1 << 30, None) == \
+        _lib.SGB_ERR_SHAPE
+    assert lib.sgb_pobtaf(ctypes.byref(m), 1, 9, 0x1000, 1 << 20, None, None) == _lib.SGB_ERR_ARG
+
+
+def test_error_mapping():
+    with pytest.raises(ValueError):
+        _lib.raise_for(_lib.SGB_ERR_SHAPE, "x")
+    with pytest.raises(TypeError):
+        _lib.raise_for(_lib.SGB_ERR_DTYPE, "x")
+    with pytest.raises(np.linalg.LinAlgError):
+        _lib.raise_for(_lib.SGB_ERR_NOT_SPD, "x")
+    with pytest.raises(NotImplementedError):
+        _lib.raise_for(_lib.SGB_ERR_UNSUPPORTED, "x")
+    _lib.raise_for(_lib.SGB_OK, "x")
