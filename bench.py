@@ -278,8 +278,8 @@ def bench_ours(args, rank: int, world: int, dist):
     # end to end through the public API with pinned host arrays
     e2e = None
     if not args.no_e2e:
-        pinned = [torch.empty(x.shape, dtype=x.dtype, pin_memory=True).numpy() for x in m.arrays()]
-        work = [torch.empty(x.shape, dtype=x.dtype, pin_memory=True).numpy() for x in m.arrays()]
+        pinned = [torch.empty(x.shape, dtype=torch.float64, pin_memory=True).numpy() for x in m.arrays()]
+        work = [torch.empty(x.shape, dtype=torch.float64, pin_memory=True).numpy() for x in m.arrays()]
         for p, x in zip(pinned, m.arrays()):
             np.copyto(p, x)
         tot = 0.0
