@@ -130,6 +130,26 @@ int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char tran
                int partial, int precision, void* workspace, size_t workspace_bytes,
                void* stream);
 
+/*
+ * sgb_pobtaf without a workspace argument, for callers that cannot allocate
+ * device memory: code running while a stream is being captured, real-time
+ * loops that forbid allocator calls, and foreign-language hosts that hold
+ * device pointers but no allocator.  This entry point has no counterpart in
+ * the reference; it computes exactly what sgb_pobtaf with precision
+ * SGB_PREC_NATIVE computes.
+ *
+ * Its scratch is a static device array of sgb_pobtaf_noalloc_scratch_bytes()
+ * bytes (64 KiB) that every GPU loading the library keeps until the process
+ * exits.  Requests whose workspace (sgb_pobtaf_workspace_size) exceeds it
+ * return SGB_ERR_WORKSPACE.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race and must be serialised by the caller.
+ * No cudaMalloc, cudaFree or other allocating routine is called.
+ */
+int sgb_pobtaf_noalloc(const sgb_bta* m, int factorize_last_block, int32_t* info, void* stream);
+size_t sgb_pobtaf_noalloc_scratch_bytes(void);
+
 /* ---- diagnostics (no counterpart in the reference) -------------------- */
 
 /* Kernel classes for sgb_profile_read. */

@@ -65,6 +65,9 @@ _SIGNATURES = {
     "sgb_pobtas": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                   ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                   ctypes.c_size_t, ctypes.c_void_p]),
+    "sgb_pobtaf_noalloc": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
+    "sgb_pobtaf_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "sgb_launch_count": (ctypes.c_longlong, []),
     "sgb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "sgb_profile_read": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
