@@ -56,8 +56,13 @@ extern "C" {
 /* Arithmetic in the storage type throughout: the drop-in form. */
 #define SGB_PREC_NATIVE 0
 /* FP64 storage; the dense block products run on the tensor cores as exact
- * bf16 slice products (fixed-point split of each FP64 operand) accumulated
- * in FP32 and summed in FP64; diagonal pivots stay in FP64.               */
+ * bf16 slice products (fixed-point split of each FP64 operand into S
+ * base-128 digits) accumulated exactly in FP32 TMEM and summed in FP64;
+ * diagonal-tile pivots stay in FP64.  S goes in bits 8-15 of the precision
+ * argument (3..7; 0 selects 5): SGB_PREC_MIXED | (S << 8).  Normwise
+ * product error ~2^-(7S+1): S=5 ~1e-11, S=7 ~1e-15.  FP64 storage only.
+ * The first 4 bytes of the workspace receive a device status word (0, or
+ * SGB_ERR_TIMEOUT if a bounded tensor-core wait gave up).                 */
 #define SGB_PREC_MIXED  1
 
 typedef struct sgb_bta {
@@ -149,6 +154,49 @@ int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char tran
  */
 int sgb_pobtaf_noalloc(const sgb_bta* m, int factorize_last_block, int32_t* info, void* stream);
 size_t sgb_pobtaf_noalloc_scratch_bytes(void);
+
+/*
+ * Row-major C <- alpha op(A) op(B) + beta C in FP64 storage with the same
+ * engines the block sweeps use (no counterpart in the reference; it is the
+ * dense product every block step of the reference performs with `@`).
+ * precision SGB_PREC_NATIVE runs on the FP64 pipe; SGB_PREC_MIXED runs the
+ * tensor-core slice products (slice count in bits 8-15 of precision, 3..7,
+ * default 5).  transA/transB are 'N' or 'T'.  The first 4 bytes of the
+ * workspace receive a device status word (0, or SGB_ERR_TIMEOUT).
+ */
+int sgb_dgemm_workspace_size(int precision, int64_t M, int64_t N, int64_t K, size_t* bytes);
+int sgb_dgemm(int precision, char transA, char transB, int64_t M, int64_t N, int64_t K, double alpha,
+              const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
+              int64_t ldc, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- batches of independent matrices ------------------------------------
+ * Many BTA matrices of uneven n, b, a and dtype processed by one graph
+ * launch (no counterpart in the reference, which handles one matrix per
+ * call).  A plan assigns the matrices to `nstreams` concurrent streams
+ * (longest first on a cost estimate), captures for every matrix
+ *   pobtaf -> pobtas 'N' -> pobtas 'T' -> pobtasi
+ * (each present if its bit is in `ops`; the solve uses the factor before
+ * the selected inversion overwrites it) into one CUDA graph, and
+ * sgb_batch_run replays it on a stream.  rhs[i] is (n*b+a, nrhs[i])
+ * row-major; precisions may be NULL (all native).  The workspace (size from
+ * sgb_batch_workspace_size with the same arguments) holds one slice per
+ * stream and an int32 info word per matrix (sgb_batch_info, device pointer,
+ * pobtaf's pivot report).  Plan creation creates and destroys streams and
+ * events and builds the graph; sgb_batch_run only launches it.            */
+#define SGB_OP_POBTAF  1
+#define SGB_OP_POBTASI 2
+#define SGB_OP_POBTAS  4
+
+typedef struct sgb_batch_plan sgb_batch_plan;
+
+int sgb_batch_workspace_size(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int count,
+                             int ops, const int* precisions, int nstreams, size_t* bytes);
+int sgb_batch_plan_create(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int count, int ops,
+                          const int* precisions, int nstreams, void* workspace, size_t workspace_bytes,
+                          sgb_batch_plan** plan);
+int sgb_batch_run(sgb_batch_plan* plan, void* stream);
+const int32_t* sgb_batch_info(const sgb_batch_plan* plan);
+int sgb_batch_plan_destroy(sgb_batch_plan* plan);
 
 /* ---- diagnostics (no counterpart in the reference) -------------------- */
 

@@ -33,6 +33,18 @@ SGB_PREC_MIXED = 1
 PRECISIONS = {"native": SGB_PREC_NATIVE, "fp64": SGB_PREC_NATIVE, "mixed": SGB_PREC_MIXED}
 
 
+def precision_code(precision) -> int:
+    """'fp64' / 'native' -> native; 'mixed' -> 5 slices; 'mixed:S' -> S slices (3..7)."""
+    if isinstance(precision, str) and precision.startswith("mixed:"):
+        S = int(precision.split(":", 1)[1])
+        if not 3 <= S <= 7:
+            raise ValueError(f"slice count must be in 3..7, got {S}")
+        return SGB_PREC_MIXED | (S << 8)
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be 'fp64', 'mixed' or 'mixed:S', got {precision!r}")
+    return PRECISIONS[precision]
+
+
 class SgbBta(ctypes.Structure):
     _fields_ = [
         ("dtype", ctypes.c_int32),
@@ -65,9 +77,26 @@ _SIGNATURES = {
     "sgb_pobtas": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                   ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                   ctypes.c_size_t, ctypes.c_void_p]),
+    "sgb_dgemm_workspace_size": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                                ctypes.POINTER(ctypes.c_size_t)]),
+    "sgb_dgemm": (ctypes.c_int, [ctypes.c_int, ctypes.c_char, ctypes.c_char, ctypes.c_int64, ctypes.c_int64,
+                                 ctypes.c_int64, ctypes.c_double, ctypes.c_void_p, ctypes.c_int64,
+                                 ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
+                                 ctypes.c_int64, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "sgb_pobtaf_noalloc": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_void_p,
                                           ctypes.c_void_p]),
     "sgb_pobtaf_noalloc_scratch_bytes": (ctypes.c_size_t, []),
+    "sgb_batch_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.POINTER(ctypes.c_void_p),
+                                                ctypes.POINTER(ctypes.c_int64), ctypes.c_int, ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_size_t)]),
+    "sgb_batch_plan_create": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.POINTER(ctypes.c_void_p),
+                                             ctypes.POINTER(ctypes.c_int64), ctypes.c_int, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
+    "sgb_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "sgb_batch_info": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "sgb_batch_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "sgb_launch_count": (ctypes.c_longlong, []),
     "sgb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "sgb_profile_read": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),

@@ -16,7 +16,9 @@ no-op).  All arithmetic runs in ``libserinv_gb300.so``; if it cannot be
 loaded or no GPU is present, the call raises — there is no CPU fallback.
 
 Extensions (keyword-only, absent from the reference): ``precision`` —
-``"fp64"`` (default, arithmetic in the storage type) or ``"mixed"``;
+``"fp64"`` (default, arithmetic in the storage type), ``"mixed"`` (FP64
+storage, block products as exact bf16 slice products on the tensor cores,
+5 slices) or ``"mixed:S"`` (S slices, 3..7; S=7 is FP64-accurate);
 ``check_spd`` (pobtaf, default True) — synchronise and raise
 ``numpy.linalg.LinAlgError`` on a non-positive pivot, like SciPy's
 ``cholesky`` in the reference.
@@ -133,14 +135,19 @@ def _bta_struct(D, Lo, Ar, T):
 
 
 def _precision(kwargs) -> int:
-    p = kwargs.get("precision", "fp64")
-    if p not in _lib.PRECISIONS:
-        raise ValueError(f"precision must be one of {sorted(_lib.PRECISIONS)}, got {p!r}")
-    return _lib.PRECISIONS[p]
+    return _lib.precision_code(kwargs.get("precision", "fp64"))
 
 
 def _workspace(nbytes: int, device) -> torch.Tensor:
     return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)
+
+
+def _check_status(ws: torch.Tensor, precision: int, what: str) -> None:
+    """Mixed precision: the workspace's first int32 is the device status word."""
+    if (precision & 0xFF) != _lib.SGB_PREC_MIXED:
+        return
+    code = int(ws[:4].view(torch.int32).item())
+    _lib.raise_for(code, what)
 
 
 def _stream(device) -> int:
@@ -198,6 +205,7 @@ def pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_a
                             nbytes.value, info.data_ptr(), _stream(device))
         _lib.raise_for(rc, "pobtaf")
         _finish(w)
+        _check_status(ws, precision, "pobtaf")
         if check:
             k = int(info.item())
             if k > 0:
@@ -234,6 +242,7 @@ def pobtasi(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_
                              _stream(device))
         _lib.raise_for(rc, "pobtasi")
         _finish(w)
+        _check_status(ws, precision, "pobtasi")
 
 
 def pobtas(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_arrow_tip_block, B, trans="N",

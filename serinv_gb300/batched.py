@@ -1,0 +1,154 @@
+"""Batches of independent BTA matrices in one graph launch.
+
+``BatchPlan(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"),
+precisions=None, nstreams=None)`` takes a list of ``(D, Lo, Ar, T)`` torch
+CUDA stacks (float32 or float64, uneven n, b, a) and optional right-hand
+sides ``(n*b+a, nrhs)``, and builds the C-level plan
+(``sgb_batch_plan_create``): the matrices are spread over ``nstreams``
+concurrent streams and their sweeps captured into one CUDA graph.
+``plan.run()`` replays it on the current stream — every array is updated in
+place exactly as by the single-matrix calls (factor, then the solve with the
+factor, then the selected inversion).
+
+``nstreams=None`` asks the autotuner (``autotune_nstreams``): it times the
+candidate stream counts on scratch copies of the same shapes and caches the
+winner in a JSON file keyed by the batch signature, so the user's data is
+never touched while tuning.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import json
+import os
+
+import torch
+
+from . import _lib
+from .algs import _bta_struct
+
+_OPS = {"pobtaf": 1, "pobtasi": 2, "pobtas": 4}
+CANDIDATES = (4, 8, 16, 32, 64)
+CACHE = os.environ.get("SGB_AUTOTUNE_CACHE",
+                       os.path.join(os.path.expanduser("~"), ".cache", "serinv_gb300", "batch_autotune.json"))
+
+
+def _signature(mats, rhs, ops, precisions) -> str:
+    parts = []
+    for i, (D, Lo, Ar, T) in enumerate(mats):
+        nr = 0 if rhs is None or rhs[i] is None else rhs[i].shape[1]
+        parts.append(f"{D.shape[0]}x{D.shape[1]}x{Ar.shape[1]}:{str(D.dtype)[6:]}:{nr}:{precisions[i]}")
+    key = ";".join(parts) + f"|ops={ops}"
+    return hashlib.sha1(key.encode()).hexdigest()
+
+
+class BatchPlan:
+    def __init__(self, mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None, nstreams=None):
+        self.lib = _lib.load()
+        self.mats = [tuple(x.contiguous() for x in m) for m in mats]
+        for m in mats:
+            for x in m:
+                if not (x.is_cuda and x.is_contiguous()):
+                    raise ValueError("batched stacks must be contiguous CUDA tensors (used in place)")
+        self.rhs = rhs
+        self.ops = sum(_OPS[o] for o in ops)
+        if precisions is None:
+            precisions = ["fp64"] * len(mats)
+        self.precisions = [_lib.precision_code(p) if m[0].dtype == torch.float64 else _lib.SGB_PREC_NATIVE
+                           for p, m in zip(precisions, mats)]
+        if nstreams is None:
+            nstreams = autotune_nstreams(mats, rhs, ops, precisions)
+        self.nstreams = int(nstreams)
+        n = len(mats)
+        self._descs = (_lib.SgbBta * n)(*[_bta_struct(*m) for m in self.mats])
+        self._rhs = (ctypes.c_void_p * n)(*[(r.data_ptr() if r is not None else None)
+                                            for r in (rhs or [None] * n)])
+        self._nrhs = (ctypes.c_int64 * n)(*[(r.shape[1] if r is not None else 0) for r in (rhs or [None] * n)])
+        self._prec = (ctypes.c_int * n)(*self.precisions)
+        nbytes = ctypes.c_size_t(0)
+        _lib.raise_for(self.lib.sgb_batch_workspace_size(self._descs, self._rhs, self._nrhs, n, self.ops,
+                                                         self._prec, self.nstreams, ctypes.byref(nbytes)),
+                       "batch workspace")
+        dev = mats[0][0].device
+        self.ws = torch.empty(nbytes.value, dtype=torch.uint8, device=dev)
+        plan = ctypes.c_void_p(0)
+        with torch.cuda.device(dev):
+            _lib.raise_for(self.lib.sgb_batch_plan_create(self._descs, self._rhs, self._nrhs, n, self.ops,
+                                                          self._prec, self.nstreams, self.ws.data_ptr(),
+                                                          nbytes.value, ctypes.byref(plan)), "batch plan")
+        self.plan = plan
+        self.device = dev
+
+    def run(self) -> None:
+        """Replay the whole batch on the current stream (asynchronous)."""
+        with torch.cuda.device(self.device):
+            _lib.raise_for(self.lib.sgb_batch_run(self.plan, torch.cuda.current_stream().cuda_stream), "batch run")
+
+    def info(self) -> torch.Tensor:
+        """Per-matrix pivot report of the last run (0 = SPD), as a host tensor (synchronises)."""
+        ptr = self.lib.sgb_batch_info(self.plan)
+        assert ptr == self.ws.data_ptr(), "the info words open the workspace"
+        return self.ws[: 4 * len(self.mats)].view(torch.int32).cpu()
+
+    def close(self) -> None:
+        if getattr(self, "plan", None):
+            self.lib.sgb_batch_plan_destroy(self.plan)
+            self.plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune_nstreams(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None,
+                      candidates=CANDIDATES, reps: int = 2) -> int:
+    """Pick the stream count by timing scratch copies of the batch; cached by signature."""
+    if precisions is None:
+        precisions = ["fp64"] * len(mats)
+    opcode = sum(_OPS[o] for o in ops)
+    sig = _signature(mats, rhs, opcode, precisions)
+    cache = {}
+    try:
+        with open(CACHE) as f:
+            cache = json.load(f)
+    except (OSError, ValueError):
+        cache = {}
+    if sig in cache:
+        return int(cache[sig])
+    scratch = [tuple(x.clone() for x in m) for m in mats]
+    srhs = None if rhs is None else [None if r is None else r.clone() for r in rhs]
+    best, best_t = None, float("inf")
+    for ns in candidates:
+        if ns > max(1, len(mats)) and best is not None:
+            break
+        times = []
+        for _ in range(reps):
+            for dst, src in zip(scratch, mats):
+                for d, s in zip(dst, src):
+                    d.copy_(s)
+            if srhs is not None:
+                for d, s in zip(srhs, rhs):
+                    if d is not None:
+                        d.copy_(s)
+            plan = BatchPlan(scratch, srhs, ops, precisions, nstreams=ns)
+            st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            st.record()
+            plan.run()
+            en.record()
+            en.synchronize()
+            times.append(st.elapsed_time(en))
+            plan.close()
+        t = min(times)
+        if t < best_t:
+            best, best_t = ns, t
+    cache[sig] = best
+    try:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        with open(CACHE, "w") as f:
+            json.dump(cache, f)
+    except OSError:
+        pass
+    return int(best)

@@ -37,10 +37,64 @@ int check_bta(const sgb_bta* m) {
     return SGB_OK;
 }
 
-int check_precision(int precision) {
-    if (precision == SGB_PREC_NATIVE) return SGB_OK;
-    if (precision == SGB_PREC_MIXED) return SGB_ERR_UNSUPPORTED;
-    return SGB_ERR_ARG;
+// precision: SGB_PREC_NATIVE, or SGB_PREC_MIXED with the slice count in
+// bits 8-15 (0 = default kDefaultSlices).  Returns the slice count (0 for
+// native) or a negative error code.
+constexpr int kDefaultSlices = 5;
+
+int parse_precision(int precision, int dtype) {
+    const int mode = precision & 0xff;
+    if (mode == SGB_PREC_NATIVE && (precision >> 8) == 0) return 0;
+    if (mode != SGB_PREC_MIXED) return -SGB_ERR_ARG;
+    int S = (precision >> 8) & 0xff;
+    if (S == 0) S = kDefaultSlices;
+    if (S < 3 || S > 7) return -SGB_ERR_ARG;
+    if (dtype != SGB_F64) return -SGB_ERR_UNSUPPORTED;
+    return S;
+}
+
+// Everything a block sweep needs besides the matrix: precision and the
+// tensor-core scratch carved from the caller's workspace.
+struct Ctx {
+    int slices = 0;          // 0: native arithmetic; 3..7: tensor-core slice products
+    void* tc = nullptr;      // slice buffers
+    size_t tc_bytes = 0;
+    int32_t* status = nullptr;  // device status word (SGB_ERR_TIMEOUT on a stuck wait)
+};
+
+// Upper bound of the tensor-core scratch of one grouped launch with up to
+// `nprob` problems whose sizes are at most mx x mx and K at most kmax.
+size_t tc_bound(int S, int64_t mx, int64_t kmax, int nprob) {
+    const int64_t Mpad = ceil_div(mx, 128) * 128, Npad = ceil_div(mx, kTcBN) * kTcBN;
+    const int64_t Kpad = ceil_div(kmax, 32) * 32 + 32;
+    const size_t per = (size_t)S * (Mpad + Npad) * Kpad * 2 + (size_t)(Mpad + Npad) * 4;
+    return (size_t)nprob * ((per + 255) / 256 * 256 + 256);
+}
+
+template <typename T>
+cudaError_t run_gemm(const Ctx& c, GemmProb<T>* pr, int np, cudaStream_t s) {
+    return gemm_simt<T>(pr, np, s);
+}
+
+// FP64: in mixed mode every product with K <= kTcMaxK goes to the tensor
+// cores; copies (no product term) and longer K stay on the FP64 pipe.
+template <>
+cudaError_t run_gemm<double>(const Ctx& c, GemmProb<double>* pr, int np, cudaStream_t s) {
+    if (c.slices == 0) return gemm_simt<double>(pr, np, s);
+    GemmProb<double> tc[kMaxProbs], simt[kMaxProbs];
+    int ntc = 0, nsimt = 0;
+    for (int i = 0; i < np; ++i) {
+        int64_t kpad = 0;
+        for (int t = 0; t < pr[i].nterms; ++t) kpad += ceil_div(pr[i].term[t].K, 32) * 32;
+        if (pr[i].nterms > 0 && kpad > 0 && kpad <= kTcMaxK && ntc < 4) tc[ntc++] = pr[i];
+        else simt[nsimt++] = pr[i];
+    }
+    if (ntc) {
+        cudaError_t e = gemm_tc(tc, ntc, c.slices, c.tc, c.tc_bytes, c.status, s);
+        if (e != cudaSuccess) return e;
+    }
+    if (nsimt) return gemm_simt<double>(simt, nsimt, s);
+    return cudaSuccess;
 }
 
 // ---- workspace layouts ------------------------------------------------
@@ -56,21 +110,31 @@ struct Carve {
 
 template <typename T>
 struct PobtafWs {
-    size_t tinv, total;
-    PobtafWs(const sgb_bta*) {
+    size_t status, tinv, tc, tc_bytes, linv, trtri, total;
+    PobtafWs(const sgb_bta* m, int S = 0) {
         Carve c;
+        status = c.take(256);
         tinv = c.take(sizeof(T) * kTile * kTile);
+        const int64_t mx = m->b > m->a ? m->b : m->a;
+        tc_bytes = S ? tc_bound(S, mx, m->b, 3) : 0;
+        tc = c.take(tc_bytes);
+        // mixed precision only: L_ii^{-1} and its triangular-inverse scratch
+        linv = c.take(S ? sizeof(T) * m->b * m->b : 0);
+        trtri = c.take(S ? sizeof(T) * kTile * m->b : 0);
         total = c.off;
     }
 };
 
 template <typename T>
 struct PobtasiWs {
-    size_t linv, linv_tip, trtri, uv, xt, w, total;
-    PobtasiWs(const sgb_bta* m) {
+    size_t status, linv, linv_tip, trtri, uv, xt, w, tc, tc_bytes, total;
+    PobtasiWs(const sgb_bta* m, int S = 0) {
         const size_t n = m->n, b = m->b, a = m->a;
         const size_t mx = b > a ? b : a;
         Carve c;
+        status = c.take(256);
+        tc_bytes = S ? tc_bound(S, (int64_t)mx, (int64_t)(b + a), 3) : 0;
+        tc = c.take(tc_bytes);
         linv = c.take(sizeof(T) * n * b * b);
         linv_tip = c.take(sizeof(T) * a * a);
         trtri = c.take(sizeof(T) * n * kTile * mx);
@@ -146,21 +210,58 @@ GemmProb<T> copy_prob(T* dst, int64_t ldd, const T* src, int64_t lds, int64_t M,
 //   [D_i; Lo_i; Ar_i] <- blocked Cholesky of the column block  (:117-139)
 //   D_{i+1} -= Lo_i Lo_i^T, Ar_{i+1} -= Ar_i Lo_i^T, T -= Ar_i Ar_i^T  (:143-159)
 template <typename T>
-int pobtaf_native(const sgb_bta* m, int factorize_last_block, void* ws, int32_t* info, cudaStream_t s) {
+int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int32_t* info, cudaStream_t s) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
     T* Ar = (T*)m->arrow;
     T* Tp = (T*)m->tip;
-    PobtafWs<T> L(m);
+    PobtafWs<T> L(m, S);
     T* tinv = (T*)((char*)ws + L.tinv);
+    Ctx cx;
+    cx.slices = S;
+    cx.tc = (char*)ws + L.tc;
+    cx.tc_bytes = L.tc_bytes;
+    cx.status = (int32_t*)((char*)ws + L.status);
     const int64_t bb = b * b, ab = a * b;
+    T* Linv = (T*)((char*)ws + L.linv);
+    T* trs = (T*)((char*)ws + L.trtri);
+
+    // [D_i; rows below] <- Cholesky of the column block.  Native: one blocked
+    // sweep over the tall column block (the TRSMs fold into the rank-32
+    // updates).  Mixed: only D_i is factored on the FP64 pipe; its inverse
+    // is formed and the TRSMs run as tensor-core products with L_ii^{-T}.
+    auto factor = [&](int64_t i, RowSet<T> r1, RowSet<T> r2) -> int {
+        T* Di = D + i * bb;
+        if (S == 0) {
+            cudaError_t e = factor_column_block<T>(Di, b, b, r1, r2, tinv, info, i * b, s);
+            return e == cudaSuccess ? SGB_OK : cuda_fail(e);
+        }
+        RowSet<T> none{nullptr, 0, b};
+        cudaError_t e = factor_column_block<T>(Di, b, b, none, none, tinv, info, i * b, s);
+        if (e == cudaSuccess) e = trtri_batched<T>(Di, b, bb, b, 1, Linv, b, bb, trs, s);
+        if (e != cudaSuccess) return cuda_fail(e);
+        GemmProb<T> pr[2];
+        int np = 0;
+        for (RowSet<T> r : {r1, r2}) {
+            if (r.rows <= 0) continue;
+            GemmProb<T> p = prob<T>();  // rows <- rows * L_ii^{-T}, in place (operands are sliced first)
+            p.M = (int32_t)r.rows;
+            p.N = (int32_t)b;
+            set_term<T>(p, 0, r.p, r.ld, 0, Linv, b, 1, b, KM_LT_N1);
+            p.Cout = r.p;
+            p.ldc = r.ld;
+            pr[np++] = p;
+        }
+        if (np) SGB_TRY(run_gemm<T>(cx, pr, np, s));
+        return SGB_OK;
+    };
 
     for (int64_t i = 0; i < n - 1; ++i) {
         RowSet<T> r1{Lo + i * bb, b, b};
         RowSet<T> r2{a ? Ar + i * ab : nullptr, a, b};
-        int rc = (int)factor_column_block<T>(D + i * bb, b, b, r1, r2, tinv, info, i * b, s);
-        if (rc != cudaSuccess) return cuda_fail((cudaError_t)rc);
+        int rc = factor(i, r1, r2);
+        if (rc != SGB_OK) return rc;
 
         const bool next_factored = (i + 1 < n - 1) || factorize_last_block;
         GemmProb<T> pr[3];
@@ -196,15 +297,15 @@ int pobtaf_native(const sgb_bta* m, int factorize_last_block, void* ws, int32_t*
             q.lower_only = factorize_last_block ? 1 : 0;
             pr[np++] = q;
         }
-        SGB_TRY(gemm_simt<T>(pr, np, s));
+        SGB_TRY(run_gemm<T>(cx, pr, np, s));
     }
 
     if (factorize_last_block) {
         const int64_t i = n - 1;
         RowSet<T> r1{nullptr, 0, b};
         RowSet<T> r2{a ? Ar + i * ab : nullptr, a, b};
-        int rc = (int)factor_column_block<T>(D + i * bb, b, b, r1, r2, tinv, info, i * b, s);
-        if (rc != cudaSuccess) return cuda_fail((cudaError_t)rc);
+        int rc = factor(i, r1, r2);
+        if (rc != SGB_OK) return rc;
         if (a) {
             GemmProb<T> q = prob<T>();  // T -= Ar_{n-1} Ar_{n-1}^T  (:177-180)
             q.M = q.N = (int32_t)a;
@@ -214,7 +315,7 @@ int pobtaf_native(const sgb_bta* m, int factorize_last_block, void* ws, int32_t*
             q.Cin = q.Cout = Tp;
             q.ldcin = q.ldc = a;
             q.lower_only = 1;
-            SGB_TRY(gemm_simt<T>(&q, 1, s));
+            SGB_TRY(run_gemm<T>(cx, &q, 1, s));
             RowSet<T> none{nullptr, 0, a};
             rc = (int)factor_column_block<T>(Tp, a, a, none, none, tinv, info, n * b, s);  // :183
             if (rc != cudaSuccess) return cuda_fail((cudaError_t)rc);
@@ -232,14 +333,19 @@ int pobtaf_native(const sgb_bta* m, int factorize_last_block, void* ws, int32_t*
 //   X_D  = (L_ii^{-T} - X_Lo^T Lo_i - X_A^T Ar_i) L_ii^{-1}                  (:167-172)
 // The last block (:114-139) is the same step without the i+1 terms.
 template <typename T>
-int pobtasi_native(const sgb_bta* m, int invert_last_block, void* ws, cudaStream_t s) {
+int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaStream_t s) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
     T* Ar = (T*)m->arrow;
     T* Tp = (T*)m->tip;
-    PobtasiWs<T> W(m);
+    PobtasiWs<T> W(m, S);
     char* base = (char*)ws;
+    Ctx cx;
+    cx.slices = S;
+    cx.tc = base + W.tc;
+    cx.tc_bytes = W.tc_bytes;
+    cx.status = (int32_t*)(base + W.status);
     T* Linv = (T*)(base + W.linv);
     T* Ltinv = (T*)(base + W.linv_tip);
     T* trs = (T*)(base + W.trtri);
@@ -259,7 +365,7 @@ int pobtasi_native(const sgb_bta* m, int invert_last_block, void* ws, cudaStream
         set_term<T>(p, 0, Ltinv, a, 1, Ltinv, a, 0, a, KM_GE_M0);
         p.Cout = Tp;
         p.ldc = a;
-        SGB_TRY(gemm_simt<T>(&p, 1, s));
+        SGB_TRY(run_gemm<T>(cx, &p, 1, s));
     }
 
     const int64_t first = invert_last_block ? n - 1 : n - 2;
@@ -299,7 +405,7 @@ int pobtasi_native(const sgb_bta* m, int invert_last_block, void* ws, cudaStream
             p.ldc = b;
             pr[np++] = p;
         }
-        if (np) SGB_TRY(gemm_simt<T>(pr, np, s));
+        if (np) SGB_TRY(run_gemm<T>(cx, pr, np, s));
 
         // (2) X_Lo = U Linv, X_A = V Linv
         np = 0;
@@ -320,7 +426,7 @@ int pobtasi_native(const sgb_bta* m, int invert_last_block, void* ws, cudaStream
             p.ldc = b;
             pr[np++] = p;
         }
-        if (np) SGB_TRY(gemm_simt<T>(pr, np, s));
+        if (np) SGB_TRY(run_gemm<T>(cx, pr, np, s));
 
         // (3) W = Linv^T - X_Lo^T Lo_i - X_A^T Ar_i
         {
@@ -336,7 +442,7 @@ int pobtasi_native(const sgb_bta* m, int invert_last_block, void* ws, cudaStream
             p.transCin = 1;
             p.Cout = Wm;
             p.ldc = b;
-            SGB_TRY(gemm_simt<T>(&p, 1, s));
+            SGB_TRY(run_gemm<T>(cx, &p, 1, s));
         }
 
         // (4) X_D = W Linv ; Lo_i <- X_Lo ; Ar_i <- X_A
@@ -351,7 +457,7 @@ int pobtasi_native(const sgb_bta* m, int invert_last_block, void* ws, cudaStream
         }
         if (has_next) pr[np++] = copy_prob<T>(Loi, b, XLo, b, b, b);
         if (a) pr[np++] = copy_prob<T>(Ari, b, XA, b, a, b);
-        SGB_TRY(gemm_simt<T>(pr, np, s));
+        SGB_TRY(run_gemm<T>(cx, pr, np, s));
     }
     return SGB_OK;
 }
@@ -510,28 +616,92 @@ int sgb_last_cuda_error(void) { return g_last_cuda_error; }
 int sgb_pobtaf_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
     int rc = check_bta(m);
     if (rc) return rc;
-    if ((rc = check_precision(precision))) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
     if (!bytes) return SGB_ERR_ARG;
-    *bytes = m->dtype == SGB_F64 ? PobtafWs<double>(m).total : PobtafWs<float>(m).total;
+    *bytes = m->dtype == SGB_F64 ? PobtafWs<double>(m, S).total : PobtafWs<float>(m, S).total;
     return SGB_OK;
 }
 
 int sgb_pobtasi_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
     int rc = check_bta(m);
     if (rc) return rc;
-    if ((rc = check_precision(precision))) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
     if (!bytes) return SGB_ERR_ARG;
-    *bytes = m->dtype == SGB_F64 ? PobtasiWs<double>(m).total : PobtasiWs<float>(m).total;
+    *bytes = m->dtype == SGB_F64 ? PobtasiWs<double>(m, S).total : PobtasiWs<float>(m, S).total;
     return SGB_OK;
 }
 
 int sgb_pobtas_workspace_size(const sgb_bta* m, int64_t nrhs, int precision, size_t* bytes) {
     int rc = check_bta(m);
     if (rc) return rc;
-    if ((rc = check_precision(precision))) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
     if (!bytes) return SGB_ERR_ARG;
     if (nrhs < 0 || nrhs > (1 << 20)) return SGB_ERR_SHAPE;
     *bytes = m->dtype == SGB_F64 ? PobtasWs<double>(m, nrhs).total : PobtasWs<float>(m, nrhs).total;
+    return SGB_OK;
+}
+
+int sgb_dgemm_workspace_size(int precision, int64_t M, int64_t N, int64_t K, size_t* bytes) {
+    const int S = parse_precision(precision, SGB_F64);
+    if (S < 0) return -S;
+    if (!bytes) return SGB_ERR_ARG;
+    if (M < 0 || N < 0 || K < 0 || M > (1 << 20) || N > (1 << 20) || K > (1 << 20)) return SGB_ERR_SHAPE;
+    if (S == 0) {
+        *bytes = 256;
+        return SGB_OK;
+    }
+    const int64_t mx = M > N ? M : N;
+    *bytes = 256 + tc_bound(S, mx, K < kTcMaxK ? K : kTcMaxK, 1);
+    return SGB_OK;
+}
+
+int sgb_dgemm(int precision, char transA, char transB, int64_t M, int64_t N, int64_t K, double alpha,
+              const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+              void* workspace, size_t workspace_bytes, void* stream) {
+    const int S = parse_precision(precision, SGB_F64);
+    if (S < 0) return -S;
+    if ((transA != 'N' && transA != 'T') || (transB != 'N' && transB != 'T')) return SGB_ERR_ARG;
+    if (M < 0 || N < 0 || K < 0 || M > (1 << 20) || N > (1 << 20) || K > (1 << 20)) return SGB_ERR_SHAPE;
+    if (M == 0 || N == 0) return SGB_OK;
+    if (C == nullptr || (K > 0 && (A == nullptr || B == nullptr))) return SGB_ERR_ARG;
+    if (ldc < N || (K > 0 && (lda < (transA == 'N' ? K : M) || ldb < (transB == 'N' ? N : K)))) return SGB_ERR_SHAPE;
+    size_t need = 0;
+    sgb_dgemm_workspace_size(precision, M, N, K, &need);
+    int rc = check_ws(workspace, workspace_bytes, need);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));
+    Ctx cx;
+    cx.slices = S;
+    cx.tc = (char*)workspace + 256;
+    cx.tc_bytes = workspace_bytes - 256;
+    cx.status = (int32_t*)workspace;
+    // K beyond the exact-accumulation bound runs as consecutive K chunks
+    // accumulated into C (beta = 1 after the first chunk).
+    const int64_t kchunk = S ? kTcMaxK : (K > 0 ? K : 1);
+    int64_t k0 = 0;
+    do {
+        const int64_t kc = (K - k0) < kchunk ? (K - k0) : kchunk;
+        GemmProb<double> p = prob<double>();
+        p.M = (int32_t)M;
+        p.N = (int32_t)N;
+        if (kc > 0) {
+            const double* Ak = transA == 'N' ? A + k0 : A + k0 * lda;
+            const double* Bk = transB == 'N' ? B + k0 * ldb : B + k0;
+            set_term<double>(p, 0, Ak, lda, transA == 'T', Bk, ldb, transB == 'T', kc);
+        }
+        p.alpha = alpha;
+        p.beta = k0 == 0 ? beta : 1.0;
+        p.Cin = C;
+        p.ldcin = ldc;
+        p.Cout = C;
+        p.ldc = ldc;
+        SGB_TRY(run_gemm<double>(cx, &p, 1, s));
+        k0 += kc;
+    } while (k0 < K);
     return SGB_OK;
 }
 
@@ -539,34 +709,39 @@ int sgb_pobtaf(const sgb_bta* m, int factorize_last_block, int precision, void* 
                size_t workspace_bytes, int32_t* info, void* stream) {
     int rc = check_bta(m);
     if (rc) return rc;
-    if ((rc = check_precision(precision))) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
     size_t need = 0;
     sgb_pobtaf_workspace_size(m, precision, &need);
     if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
-    if (m->dtype == SGB_F64) return pobtaf_native<double>(m, factorize_last_block, workspace, info, s);
-    return pobtaf_native<float>(m, factorize_last_block, workspace, info, s);
+    SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
+    if (m->dtype == SGB_F64) return pobtaf_run<double>(m, factorize_last_block, S, workspace, info, s);
+    return pobtaf_run<float>(m, factorize_last_block, S, workspace, info, s);
 }
 
 int sgb_pobtasi(const sgb_bta* m, int invert_last_block, int precision, void* workspace, size_t workspace_bytes,
                 void* stream) {
     int rc = check_bta(m);
     if (rc) return rc;
-    if ((rc = check_precision(precision))) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
     size_t need = 0;
     sgb_pobtasi_workspace_size(m, precision, &need);
     if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
-    if (m->dtype == SGB_F64) return pobtasi_native<double>(m, invert_last_block, workspace, s);
-    return pobtasi_native<float>(m, invert_last_block, workspace, s);
+    SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
+    if (m->dtype == SGB_F64) return pobtasi_run<double>(m, invert_last_block, S, workspace, s);
+    return pobtasi_run<float>(m, invert_last_block, S, workspace, s);
 }
 
 int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char trans, int partial, int precision,
                void* workspace, size_t workspace_bytes, void* stream) {
     int rc = check_bta(m);
     if (rc) return rc;
-    if ((rc = check_precision(precision))) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
     if (trans != 'N' && trans != 'T' && trans != 'C') return SGB_ERR_ARG;
     if (nrhs < 0 || nrhs > (1 << 20) || ldb < nrhs) return SGB_ERR_SHAPE;
     if (nrhs > 0 && rhs == nullptr) return SGB_ERR_ARG;

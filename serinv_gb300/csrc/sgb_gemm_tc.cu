@@ -1,0 +1,735 @@
+// Tensor-core (tcgen05) FP64-storage GEMM built from exact bf16 slice products.
+//
+// Each FP64 operand row (rows of op(A), columns of op(B)) is scaled by a
+// power of two 2^e so its entries lie in (-1, 1), turned into a signed
+// fixed-point integer X = round(x * 2^(7S)), and cut into S balanced base-128
+// digits d_0 .. d_{S-1} (|d_0| <= 128, |d_p| <= 64).  Slice p stores
+// w_p = d_p * 2^(-7p) in bf16 (exact: at most 8 significant bits).  Then
+//
+//   C[m][n] = 2^(eA[m] + eB[n] - 14) * sum_{p+q <= S-1} (A_p B_q)[m][n]
+//
+// The products are exact in the FP32 accumulator; grouping them by level
+// l = p + q keeps every partial sum of a level an integer multiple of
+// 2^(-7l) whose magnitude stays below 2^24 of those units: per k a level-l
+// term is at most 2^14 + (l-1) 2^12 units, so levels 0..4 are exact for
+// K <= kTcMaxK = 576.  Each level up to 4 has its own TMEM accumulator; for
+// S = 7 the last accumulator also takes levels 5 and 6 (weight <= 2^-35).
+// The truncation error of S digits is 2^-(7S+1) of the row maximum.  The
+// epilogue adds the accumulators exactly as an FP32 pair (two-sum), widens
+// the pair with integer bit operations, adds it in FP64 (one FP64 add),
+// applies the power-of-two scale on the exponent bits and alpha/beta, and
+// stores FP64: two FP64 instructions per element, because every FP64 warp
+// instruction occupies its SM quarter for ~64 cycles on this part.
+//
+// This is the published Ozaki error-free splitting idea (Ozaki, Ogita,
+// Oishi, Rump) specialised to fixed-point digits and level-grouped exact
+// tensor-core accumulation.
+//
+// Kernel structure (one CTA = one 128 x BN output tile, 128 threads):
+//   * operand slices are staged in shared memory in the no-swizzle K-major
+//     core-matrix layout (8 rows x 16 bytes per core matrix) by cp.async,
+//     two stages;
+//   * thread 0 issues tcgen05.mma (cta_group::1, kind::f16, bf16 inputs,
+//     FP32 accumulation in TMEM) and tcgen05.commit to an mbarrier per stage;
+//   * all mbarrier waits are bounded; on timeout an error word is set and the
+//     kernel drains (bounded) and frees its TMEM before returning;
+//   * the four warps read their 32 TMEM lanes with tcgen05.ld and write FP64.
+#include <cuda_bf16.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "sgb_internal.cuh"
+
+namespace sgb {
+
+namespace {
+
+constexpr int TC_BM = 128;
+constexpr int TC_BK = 32;
+constexpr int TC_THREADS = 128;
+constexpr int kMaxTcProbs = 4;
+constexpr int kMaxSplitJobs = 2 * kMaxTcProbs * 2;  // probs x operands x terms
+constexpr long long kSpinLimit = 1ll << 22;         // bounded mbarrier waits (~1 s)
+
+// ---------------------------------------------------------------- split
+
+struct SplitSrc {
+    const double* X;
+    int64_t ld_r, ld_k;   // element (r, k) at X[r*ld_r + k*ld_k]
+    int64_t stride;       // batch stride (elements)
+    int32_t K, koff;      // source K extent; destination K offset (multiple of TC_BK)
+};
+
+struct SplitJob {
+    SplitSrc src;
+    __nv_bfloat16* out;   // [S][Rpad][Kpad] per instance
+    int32_t* exps;        // [Rpad] per instance (biased FP64 exponent of the row max)
+    int64_t out_stride, exp_stride;
+    int32_t R, Rpad, Kpad;
+    int32_t batch;
+    int32_t tiles_r, tiles_k, tile_begin;
+};
+
+struct SplitLaunch {
+    SplitJob j[kMaxSplitJobs];
+    int32_t nj;
+    int32_t S;
+};
+
+__device__ __forceinline__ int find_job(const SplitLaunch& L, int tile) {
+    int ji = 0;
+#pragma unroll 1
+    for (int q = 1; q < L.nj; ++q)
+        if (tile >= L.j[q].tile_begin) ji = q;
+    return ji;
+}
+
+// Load a 32 x 32 tile of the source into shared memory, coalesced along
+// whichever index is contiguous.  Elements outside the source are zero.
+__device__ __forceinline__ void load_tile(const SplitJob& J, int inst, int r0, int k0, double (*t)[33]) {
+    const double* X = J.src.X + (int64_t)inst * J.src.stride;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+    if (J.src.ld_k == 1) {
+        for (int rr = ty; rr < 32; rr += 8) {
+            const int r = r0 + rr, k = k0 + tx;
+            t[rr][tx] = (r < J.R && k < J.src.K) ? X[(int64_t)r * J.src.ld_r + k] : 0.0;
+        }
+    } else {
+        for (int kk = ty; kk < 32; kk += 8) {
+            const int r = r0 + tx, k = k0 + kk;
+            t[tx][kk] = (r < J.R && k < J.src.K) ? X[(int64_t)r * J.src.ld_r + (int64_t)k * J.src.ld_k] : 0.0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_split_exp(const __grid_constant__ SplitLaunch L) {
+    __shared__ double t[32][33];
+    const int tile = blockIdx.x;
+    const SplitJob& J = L.j[find_job(L, tile)];
+    int local = tile - J.tile_begin;
+    const int per = J.tiles_r * J.tiles_k;
+    const int inst = local / per;
+    local -= inst * per;
+    const int r0 = (local / J.tiles_k) * 32;
+    const int k0 = (local % J.tiles_k) * 32;
+    if (k0 >= J.src.K || r0 >= J.R) return;
+    load_tile(J, inst, r0, k0, t);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int rr = threadIdx.x;
+        int emax = 0;
+        for (int kk = 0; kk < 32; ++kk) {
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(t[rr][kk]);
+            const int e = (int)((bits >> 52) & 0x7ff);
+            emax = e > emax ? e : emax;
+        }
+        if (r0 + rr < J.R && emax > 0) atomicMax(J.exps + (int64_t)inst * J.exp_stride + r0 + rr, emax);
+    }
+}
+
+// Balanced base-128 digits of x scaled by the row exponent Erow (biased).
+template <int S>
+__device__ __forceinline__ void digits(double x, int Erow, int (&d)[S]) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int Ex = (int)((bits >> 52) & 0x7ff);
+#pragma unroll
+    for (int p = 0; p < S; ++p) d[p] = 0;
+    if (Ex == 0 || Erow == 0) return;  // zero, subnormal (flushed) or zero row
+    const long long m = (long long)((bits & ((1ull << 52) - 1)) | (1ull << 52));
+    const int rs = Erow - Ex + 53 - 7 * S;  // right shift; >= 53 - 7S > 0 for S <= 7
+    long long X;
+    if (rs >= 62) X = 0;
+    else if (rs <= 0) X = m << (-rs);
+    else X = (m + (1ll << (rs - 1))) >> rs;
+    if (bits >> 63) X = -X;
+#pragma unroll
+    for (int p = S - 1; p >= 1; --p) {
+        int v = (int)(X & 127);
+        if (v >= 64) v -= 128;
+        d[p] = v;
+        X = (X - v) >> 7;
+    }
+    d[0] = (int)X;
+}
+
+template <int S>
+__global__ void __launch_bounds__(256) k_split_slices(const __grid_constant__ SplitLaunch L) {
+    __shared__ double t[32][33];
+    __shared__ int ex[32];
+    const int tile = blockIdx.x;
+    const SplitJob& J = L.j[find_job(L, tile)];
+    int local = tile - J.tile_begin;
+    const int per = J.tiles_r * J.tiles_k;
+    const int inst = local / per;
+    local -= inst * per;
+    const int r0 = (local / J.tiles_k) * 32;
+    const int k0 = (local % J.tiles_k) * 32;  // within this source's padded K range
+    load_tile(J, inst, r0, k0, t);
+    if (threadIdx.x < 32) {
+        const int r = r0 + threadIdx.x;
+        ex[threadIdx.x] = r < J.R ? J.exps[(int64_t)inst * J.exp_stride + r] : 0;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    __nv_bfloat16* out = J.out + (int64_t)inst * J.out_stride;
+    const int64_t slice = (int64_t)J.Rpad * J.Kpad;
+    for (int rr = ty; rr < 32; rr += 8) {
+        const int r = r0 + rr;
+        if (r >= J.Rpad) continue;
+        int d[S];
+        digits<S>(t[rr][tx], ex[rr], d);
+        const int64_t o = (int64_t)r * J.Kpad + J.src.koff + k0 + tx;
+#pragma unroll
+        for (int p = 0; p < S; ++p) {
+            const float w = ldexpf((float)d[p], -7 * p);
+            out[p * slice + o] = __float2bfloat16_rn(w);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- tcgen05 GEMM
+
+struct TcProb {
+    const __nv_bfloat16* A;  // [S][Mpad][Kpad]
+    const __nv_bfloat16* B;  // [S][Npad][Kpad]
+    const int32_t* eA;
+    const int32_t* eB;
+    const double* Cin;
+    double* Cout;
+    int64_t strideA, strideB, strideEA, strideEB, strideCin, strideC;
+    int64_t ldcin, ldc;
+    double alpha, beta;
+    int32_t M, N, Mpad, Npad, Kpad;
+    int32_t batch;
+    int32_t lower_only, transCin;
+    int32_t tiles_m, tiles_n, tile_begin;
+};
+
+struct TcLaunch {
+    TcProb p[kMaxTcProbs];
+    int32_t np;
+    int32_t* err;  // set to SGB_ERR_TIMEOUT if a bounded wait gave up
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// tcgen05 shared-memory matrix descriptor, no swizzle, K-major.
+// bits 0-13 start>>4, 16-29 LBO>>4 (K-direction core-matrix stride),
+// 32-45 SBO>>4 (M/N-direction core-matrix stride), 46-47 version = 1,
+// 61-63 layout = 0 (no swizzle).
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3fff);
+    d |= (uint64_t)((lbo >> 4) & 0x3fff) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3fff) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N>>3 at bit 17, M>>4 at bit 24.
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: returns false if the phase did not complete in time.
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+    for (long long i = 0; i < kSpinLimit; ++i)
+        if (mbar_try(addr, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accum) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// FP32 -> FP64 by bit operations (exact; zero and subnormal inputs give 0):
+// keeps the conversion off the FP64 pipe.
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t ex = (u >> 23) & 0xffu;
+    if (ex == 0u) return 0.0;
+    const uint32_t hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    const uint32_t lo = (u & 0x7u) << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// r * 2^e on the exponent bits when the result stays normal, else ldexp.
+__device__ __forceinline__ double scale_pow2(double r, int e) {
+    const long long bits = __double_as_longlong(r);
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    if (ex == 0) return r;  // zero
+    const int nx = ex + e;
+    if (nx > 0 && nx < 2047) return __longlong_as_double(bits + ((long long)e << 52));
+    return ldexp(r, e);
+}
+
+template <int S, int BN>
+struct TcSmem {
+    static constexpr int kA = S * TC_BM * TC_BK * 2;   // bytes of A slices per stage
+    static constexpr int kB = S * BN * TC_BK * 2;      // bytes of B slices per stage
+    static constexpr int kStage = kA + kB;
+    static constexpr int kBytes = 2 * kStage + 1024 + 64;
+};
+
+template <int S, int BN>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_gemm_tc(const __grid_constant__ TcLaunch L) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned carve
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    using SM = TcSmem<S, BN>;
+    uint64_t* bars = (uint64_t*)(smem + 2 * SM::kStage);  // bars[0], bars[1]
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2);
+
+    const int tile = blockIdx.x;
+    int pi = 0;
+#pragma unroll 1
+    for (int q = 1; q < L.np; ++q)
+        if (tile >= L.p[q].tile_begin) pi = q;
+    const TcProb& P = L.p[pi];
+    int local = tile - P.tile_begin;
+    const int per = P.tiles_m * P.tiles_n;
+    const int inst = local / per;
+    local -= inst * per;
+    const int m0 = (local / P.tiles_n) * TC_BM;
+    const int n0 = (local % P.tiles_n) * BN;
+    if (P.lower_only && n0 >= m0 + TC_BM) return;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    constexpr int NACC = S < 6 ? S : 6;  // TMEM accumulators (levels 0..NACC-1, last one lumps the rest)
+    constexpr int kUsed = NACC * BN;
+    constexpr int kCols = kUsed <= 32 ? 32 : kUsed <= 64 ? 64 : kUsed <= 128 ? 128 : kUsed <= 256 ? 256 : 512;
+    static_assert(kUsed <= 512, "TMEM columns");
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(smem_u32(&bars[0]), 1);
+        mbar_init(smem_u32(&bars[1]), 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    const __nv_bfloat16* Ag = P.A + (int64_t)inst * P.strideA;
+    const __nv_bfloat16* Bg = P.B + (int64_t)inst * P.strideB;
+    const int64_t sliceA = (int64_t)P.Mpad * P.Kpad;
+    const int64_t sliceB = (int64_t)P.Npad * P.Kpad;
+    const int nkb = P.Kpad / TC_BK;
+    constexpr uint32_t idesc = make_idesc(TC_BM, BN);
+    const uint32_t sbase = smem_u32(smem);
+    bool ok = true;
+    uint32_t inited = 0;  // bit l: accumulator l written (thread 0 only)
+
+    for (int kb = 0; kb < nkb; ++kb) {
+        const int st = kb & 1;
+        if (kb >= 2) {
+            if (!mbar_wait(smem_u32(&bars[st]), (uint32_t)(((kb - 2) >> 1) & 1))) ok = false;
+        }
+        if (__syncthreads_or(!ok)) break;
+        const uint32_t sA = sbase + st * SM::kStage;
+        const uint32_t sB = sA + SM::kA;
+        const int k0 = kb * TC_BK;
+        // A: S slices x 128 rows x 4 chunks of 8 elements
+        constexpr int nA = S * TC_BM * 4;
+        constexpr int nB = S * BN * 4;
+        for (int c = tid; c < nA + nB; c += TC_THREADS) {
+            if (c < nA) {
+                const int p = c / (TC_BM * 4);
+                const int rem = c - p * TC_BM * 4;
+                const int r = rem >> 2, kc = rem & 3;
+                const __nv_bfloat16* src = Ag + p * sliceA + (int64_t)(m0 + r) * P.Kpad + k0 + kc * 8;
+                const uint32_t dst = sA + p * (TC_BM * TC_BK * 2) + (kc * (TC_BM / 8) + (r >> 3)) * 128 + (r & 7) * 16;
+                cp_async16(dst, src);
+            } else {
+                const int cc = c - nA;
+                const int q = cc / (BN * 4);
+                const int rem = cc - q * BN * 4;
+                const int r = rem >> 2, kc = rem & 3;
+                const __nv_bfloat16* src = Bg + q * sliceB + (int64_t)(n0 + r) * P.Kpad + k0 + kc * 8;
+                const uint32_t dst = sB + q * (BN * TC_BK * 2) + (kc * (BN / 8) + (r >> 3)) * 128 + (r & 7) * 16;
+                cp_async16(dst, src);
+            }
+        }
+        asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int s = 0; s < TC_BK / 16; ++s) {
+#pragma unroll
+                for (int p = 0; p < S; ++p) {
+                    const uint64_t ad = make_desc(sA + p * (TC_BM * TC_BK * 2) + s * 2 * (TC_BM / 8) * 128,
+                                                  (TC_BM / 8) * 128, 128);
+#pragma unroll
+                    for (int q = 0; q + p < S; ++q) {
+                        const int l = (p + q) < NACC ? (p + q) : NACC - 1;
+                        const uint64_t bd = make_desc(sB + q * (BN * TC_BK * 2) + s * 2 * (BN / 8) * 128,
+                                                      (BN / 8) * 128, 128);
+                        tc_mma(tmem + l * BN, ad, bd, idesc, (inited >> l) & 1u);
+                        inited |= 1u << l;
+                    }
+                }
+            }
+            tc_commit(smem_u32(&bars[st]));
+        }
+    }
+
+    // wait for the last commit (covers every MMA issued before it)
+    if (ok && nkb > 0) {
+        const int kl = nkb - 1;
+        if (!mbar_wait(smem_u32(&bars[kl & 1]), (uint32_t)((kl >> 1) & 1))) ok = false;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool all_ok = !__syncthreads_or(!ok);
+
+    if (all_ok) {
+        const int m = m0 + warp * 32 + lane;
+        const int64_t mrow = m;
+        const int eAm = (m < P.M) ? P.eA[(int64_t)inst * P.strideEA + m] : 0;
+        double* C = P.Cout + (int64_t)inst * P.strideC;
+        const double* Ci = P.Cin ? P.Cin + (int64_t)inst * P.strideCin : nullptr;
+        const int32_t* eB = P.eB + (int64_t)inst * P.strideEB;
+        const bool neg = P.alpha == -1.0, unit = P.alpha == 1.0 || neg;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            float v[NACC][16];
+            const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + c0;
+            if (nkb > 0) {
+#pragma unroll
+                for (int l = 0; l < NACC; ++l) tmem_ld16(ta + l * BN, v[l]);
+            } else {
+#pragma unroll
+                for (int l = 0; l < NACC; ++l)
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) v[l][i] = 0.f;
+            }
+            if (m < P.M) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int n = n0 + c0 + i;
+                    if (n >= P.N) break;
+                    if (P.lower_only && n > m) continue;
+                    double r = 0.0;
+                    const int eBn = eB[n];
+                    if (eAm != 0 && eBn != 0) {
+                        // exact FP32-pair sum of the level accumulators
+                        float hi = v[0][i], lo = 0.f;
+#pragma unroll
+                        for (int l = 1; l < NACC; ++l) {
+                            const float s2 = hi + v[l][i];
+                            const float bb = s2 - hi;
+                            lo += (hi - (s2 - bb)) + (v[l][i] - bb);
+                            hi = s2;
+                        }
+                        const float h2 = hi + lo;
+                        lo = lo - (h2 - hi);
+                        hi = h2;
+                        r = f32_to_f64(hi) + f32_to_f64(lo);
+                        r = scale_pow2(r, eAm + eBn - 2058);
+                    }
+                    if (!unit) r *= P.alpha;
+                    else if (neg) r = -r;
+                    if (Ci != nullptr && P.beta != 0.0) {
+                        const double cv = P.transCin ? Ci[(int64_t)n * P.ldcin + mrow] : Ci[mrow * P.ldcin + n];
+                        r = fma(P.beta, cv, r);
+                    }
+                    C[mrow * P.ldc + n] = r;
+                }
+            }
+        }
+    } else if (tid == 0 && L.err != nullptr) {
+        atomicExch(L.err, SGB_ERR_TIMEOUT);
+    }
+
+    if (!all_ok) {
+        // drain: MMAs may still be in flight; wait (bounded) on both stages
+        // before the TMEM is released.
+        if (tid == 0) {
+            for (int st = 0; st < 2; ++st) {
+                const uint32_t a = smem_u32(&bars[st]);
+                mbar_wait(a, 0);
+                mbar_wait(a, 1);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    }
+}
+
+template <int S, int BN>
+cudaError_t set_smem_attr() {
+    return cudaFuncSetAttribute(k_gemm_tc<S, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                TcSmem<S, BN>::kBytes);
+}
+
+template <int S, int BN>
+cudaError_t launch_tc(TcLaunch& L, int total_tiles, cudaStream_t s) {
+    k_gemm_tc<S, BN><<<total_tiles, TC_THREADS, TcSmem<S, BN>::kBytes, s>>>(L);
+    return cudaGetLastError();
+}
+
+std::mutex g_attr_mu;
+bool g_attr_done[64] = {};
+
+}  // namespace
+
+// ---------------------------------------------------------------- host
+
+cudaError_t tc_prepare() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    if (g_attr_done[dev]) return cudaSuccess;
+    for (cudaError_t x : {set_smem_attr<3, 64>(), set_smem_attr<4, 64>(), set_smem_attr<5, 64>(),
+                          set_smem_attr<6, 64>(), set_smem_attr<7, 64>(), set_smem_attr<3, 32>(),
+                          set_smem_attr<4, 32>(), set_smem_attr<5, 32>(), set_smem_attr<6, 32>(),
+                          set_smem_attr<7, 32>()})
+        if (x != cudaSuccess) return x;
+    g_attr_done[dev] = true;
+    return cudaSuccess;
+}
+
+size_t tc_workspace_bytes(const GemmProb<double>* probs, int np, int S) {
+    size_t total = 0;
+    for (int i = 0; i < np; ++i) {
+        const GemmProb<double>& p = probs[i];
+        if (p.M <= 0 || p.N <= 0 || p.batch <= 0) continue;
+        int64_t Kpad = 0;
+        for (int t = 0; t < p.nterms; ++t) Kpad += ceil_div(p.term[t].K, TC_BK) * TC_BK;
+        if (Kpad == 0) Kpad = TC_BK;
+        const int64_t Mpad = ceil_div(p.M, TC_BM) * TC_BM;
+        const int64_t Npad = ceil_div(p.N, kTcBN) * kTcBN;
+        const size_t per = (size_t)S * (Mpad + Npad) * Kpad * 2 + (size_t)(Mpad + Npad) * 4;
+        total += (per * p.batch + 255) / 256 * 256 + 256;
+    }
+    return total;
+}
+
+cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_bytes, int32_t* err,
+                    cudaStream_t s) {
+    if (np > kMaxTcProbs) return cudaErrorInvalidValue;
+    if (S != 3 && S != 4 && S != 5 && S != 6 && S != 7) return cudaErrorInvalidValue;
+    SplitLaunch SL;
+    memset(&SL, 0, sizeof(SL));
+    SL.S = S;
+    TcLaunch TL;
+    memset(&TL, 0, sizeof(TL));
+    TL.err = err;
+    char* base = (char*)ws;
+    size_t off = 0;
+    int64_t split_tiles = 0, gemm_tiles = 0;
+    // 128 x 64 tiles unless that leaves most SMs idle; then 128 x 32.
+    int64_t tiles64 = 0;
+    for (int i = 0; i < np; ++i)
+        if (probs[i].M > 0 && probs[i].N > 0 && probs[i].batch > 0)
+            tiles64 += ceil_div(probs[i].M, TC_BM) * ceil_div(probs[i].N, kTcBN) * probs[i].batch;
+    const int bn = tiles64 < 148 ? 32 : 64;
+    struct ExpRange { int32_t* p; size_t bytes; };
+    ExpRange ranges[kMaxTcProbs * 2];
+    int nranges = 0;
+    for (int i = 0; i < np; ++i) {
+        const GemmProb<double>& p = probs[i];
+        if (p.M <= 0 || p.N <= 0 || p.batch <= 0) continue;
+        int64_t Kpad = 0;
+        for (int t = 0; t < p.nterms; ++t) Kpad += ceil_div(p.term[t].K, TC_BK) * TC_BK;
+        const int64_t Kalloc = Kpad == 0 ? TC_BK : Kpad;
+        if (Kpad > kTcMaxK) return cudaErrorInvalidValue;
+        const int64_t Mpad = ceil_div(p.M, TC_BM) * TC_BM;
+        const int64_t Npad = ceil_div(p.N, kTcBN) * kTcBN;
+        const size_t bytesA = (size_t)S * Mpad * Kalloc * 2, bytesB = (size_t)S * Npad * Kalloc * 2;
+        const size_t per = bytesA + bytesB + (size_t)(Mpad + Npad) * 4;
+        const size_t per_al = (per + 255) / 256 * 256;
+        if (off + per_al * p.batch + 256 > ws_bytes) return cudaErrorInvalidValue;
+        __nv_bfloat16* As = (__nv_bfloat16*)(base + off);
+        __nv_bfloat16* Bs = (__nv_bfloat16*)(base + off + bytesA);
+        int32_t* eA = (int32_t*)(base + off + bytesA + bytesB);
+        int32_t* eB = eA + Mpad;
+        ranges[nranges++] = ExpRange{eA, 0};
+        // exps live inside each instance block; zero them per instance below
+        const int64_t inst_stride_bytes = (int64_t)per_al;
+        // split jobs: one per (operand, term)
+        int32_t koff = 0;
+        for (int t = 0; t < p.nterms; ++t) {
+            const GemmTerm<double>& tm = p.term[t];
+            if (tm.K <= 0) continue;
+            // op(A_t): row m, column k
+            SplitJob ja;
+            memset(&ja, 0, sizeof(ja));
+            ja.src.X = tm.A;
+            ja.src.ld_r = tm.transA ? 1 : tm.lda;
+            ja.src.ld_k = tm.transA ? tm.lda : 1;
+            ja.src.stride = tm.strideA;
+            ja.src.K = tm.K;
+            ja.src.koff = koff;
+            ja.out = As;
+            ja.exps = eA;
+            ja.out_stride = inst_stride_bytes / 2;
+            ja.exp_stride = inst_stride_bytes / 4;
+            ja.R = p.M;
+            ja.Rpad = (int32_t)Mpad;
+            ja.Kpad = (int32_t)Kalloc;
+            ja.batch = p.batch;
+            ja.tiles_r = (int32_t)ceil_div(Mpad, 32);
+            ja.tiles_k = (int32_t)ceil_div(tm.K, TC_BK);
+            // op(B_t): row n (column of op(B)), column k
+            SplitJob jb = ja;
+            jb.src.X = tm.B;
+            jb.src.ld_r = tm.transB ? tm.ldb : 1;
+            jb.src.ld_k = tm.transB ? 1 : tm.ldb;
+            jb.src.stride = tm.strideB;
+            jb.out = Bs;
+            jb.exps = eB;
+            jb.R = p.N;
+            jb.Rpad = (int32_t)Npad;
+            jb.tiles_r = (int32_t)ceil_div(Npad, 32);
+            for (SplitJob* j : {&ja, &jb}) {
+                if (SL.nj >= kMaxSplitJobs) return cudaErrorInvalidValue;
+                j->tile_begin = (int32_t)split_tiles;
+                split_tiles += (int64_t)j->tiles_r * j->tiles_k * j->batch;
+                SL.j[SL.nj++] = *j;
+            }
+            koff += (int32_t)(ceil_div(tm.K, TC_BK) * TC_BK);
+        }
+        TcProb tp;
+        memset(&tp, 0, sizeof(tp));
+        tp.A = As;
+        tp.B = Bs;
+        tp.eA = eA;
+        tp.eB = eB;
+        tp.Cin = p.Cin;
+        tp.Cout = p.Cout;
+        tp.strideA = tp.strideB = inst_stride_bytes / 2;
+        tp.strideEA = tp.strideEB = inst_stride_bytes / 4;
+        tp.strideCin = p.strideCin;
+        tp.strideC = p.strideC;
+        tp.ldcin = p.ldcin;
+        tp.ldc = p.ldc;
+        tp.alpha = p.alpha;
+        tp.beta = p.beta;
+        tp.M = p.M;
+        tp.N = p.N;
+        tp.Mpad = (int32_t)Mpad;
+        tp.Npad = (int32_t)Npad;
+        tp.Kpad = (int32_t)Kpad;
+        tp.batch = p.batch;
+        tp.lower_only = p.lower_only;
+        tp.transCin = p.transCin;
+        tp.tiles_m = (int32_t)(Mpad / TC_BM);
+        tp.tiles_n = (int32_t)(Npad / bn);
+        tp.tile_begin = (int32_t)gemm_tiles;
+        gemm_tiles += (int64_t)tp.tiles_m * tp.tiles_n * p.batch;
+        TL.p[TL.np++] = tp;
+        // the whole instance block (slices + exps) is zeroed: padding slices
+        // beyond the sources and the exponent maxima must start at zero
+        ranges[nranges - 1].bytes = per_al * p.batch;
+        ranges[nranges - 1].p = (int32_t*)As;
+        off += per_al * p.batch;
+    }
+    if (TL.np == 0) return cudaSuccess;
+    for (int r = 0; r < nranges; ++r) {
+        cudaError_t e = cudaMemsetAsync(ranges[r].p, 0, ranges[r].bytes, s);
+        if (e != cudaSuccess) return e;
+    }
+    if (split_tiles > 0) {
+        prof_before(s);
+        k_split_exp<<<(unsigned)split_tiles, 256, 0, s>>>(SL);
+        prof_after(SGB_KCLASS_SPLIT, s, 0.0);
+        prof_before(s);
+        switch (S) {
+            case 3: k_split_slices<3><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
+            case 4: k_split_slices<4><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
+            case 5: k_split_slices<5><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
+            case 6: k_split_slices<6><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
+            default: k_split_slices<7><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
+        }
+        prof_after(SGB_KCLASS_SPLIT, s, 0.0);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    double fl = 0.0;
+    for (int i = 0; i < np; ++i) fl += useful_flops<double>(probs[i]);
+    cudaError_t e = tc_prepare();
+    if (e != cudaSuccess) return e;
+    prof_before(s);
+    if (bn == 64) {
+        switch (S) {
+            case 3: e = launch_tc<3, 64>(TL, (int)gemm_tiles, s); break;
+            case 4: e = launch_tc<4, 64>(TL, (int)gemm_tiles, s); break;
+            case 5: e = launch_tc<5, 64>(TL, (int)gemm_tiles, s); break;
+            case 6: e = launch_tc<6, 64>(TL, (int)gemm_tiles, s); break;
+            default: e = launch_tc<7, 64>(TL, (int)gemm_tiles, s); break;
+        }
+    } else {
+        switch (S) {
+            case 3: e = launch_tc<3, 32>(TL, (int)gemm_tiles, s); break;
+            case 4: e = launch_tc<4, 32>(TL, (int)gemm_tiles, s); break;
+            case 5: e = launch_tc<5, 32>(TL, (int)gemm_tiles, s); break;
+            case 6: e = launch_tc<6, 32>(TL, (int)gemm_tiles, s); break;
+            default: e = launch_tc<7, 32>(TL, (int)gemm_tiles, s); break;
+        }
+    }
+    prof_after(SGB_KCLASS_GEMM_TC, s, fl);
+    return e;
+}
+
+}  // namespace sgb

@@ -105,6 +105,20 @@ cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, i
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Tensor-core slice GEMM (sgb_gemm_tc.cu): FP64 storage, exact bf16 slice
+// products on tcgen05.  Output tiles 128 x 64 or 128 x 32 (operands are
+// padded to kTcBN); the concatenated K of a problem's terms must not exceed
+// kTcMaxK (exactness bound of the level accumulators).  `err` (device int32, may be null) receives
+// SGB_ERR_TIMEOUT if a bounded wait gives up.
+constexpr int kTcBN = 64;
+constexpr int kTcMaxK = 576;
+size_t tc_workspace_bytes(const GemmProb<double>* probs, int np, int S);
+// Sets the tensor-core kernels' shared-memory attribute on the current
+// device (once); call before capturing launches into a graph.
+cudaError_t tc_prepare();
+cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_bytes, int32_t* err,
+                    cudaStream_t s);
+
 // Launch accounting (sgb_prof.cu): call prof_before just before and
 // prof_after just after every kernel launch.
 void prof_before(cudaStream_t s);

@@ -21,56 +21,100 @@ namespace {
 constexpr int NT = 256;
 
 template <typename T>
-__device__ __forceinline__ T sgb_sqrt(T x);
+__device__ __forceinline__ T sgb_rsqrt(T x);
 template <>
-__device__ __forceinline__ double sgb_sqrt<double>(double x) { return sqrt(x); }
+__device__ __forceinline__ double sgb_rsqrt<double>(double x) { return rsqrt(x); }
 template <>
-__device__ __forceinline__ float sgb_sqrt<float>(float x) { return sqrtf(x); }
+__device__ __forceinline__ float sgb_rsqrt<float>(float x) { return rsqrtf(x); }
 
-// Inverse of the lower-triangular tile s (nb x nb) into x, one column per
-// thread of the first warp:  x[r][j] = (delta_rj - sum_{k=j}^{r-1} s[r][k] x[k][j]) / s[r][r].
+// Inverse of the lower-triangular tile s (32 x 32, identity-padded beyond
+// nb) into x, given the reciprocal diagonal yv.  Recursive doubling keeps
+// every step a small parallel product, so no thread runs a long dependent
+// chain of FP64 operations (each FP64 warp instruction costs ~64 issue
+// cycles on this part):
+//   leaves: the four 8 x 8 diagonal blocks by forward substitution;
+//   level 1: X21 = -X22 (L21 X11) for the two 16 x 16 blocks;
+//   level 2: the same for the 32 x 32 tile.
+// Requires all NT threads; ends with a barrier.
 template <typename T>
-__device__ __forceinline__ void tile_inverse(T (*s)[kTile + 1], T (*x)[kTile + 1], int nb) {
-    const int j = threadIdx.x;
-    if (j < nb) {
-        for (int r = 0; r < j; ++r) x[r][j] = T(0);
-        for (int r = j; r < nb; ++r) {
+__device__ __forceinline__ void tile_inverse(T (*s)[kTile + 1], T (*x)[kTile + 1], T (*tmp)[kTile + 1],
+                                             const T* yv) {
+    const int tid = threadIdx.x;
+    for (int e = tid; e < kTile * kTile; e += NT) x[e / kTile][e % kTile] = T(0);
+    __syncthreads();
+    if (tid < 32) {  // leaves: 4 blocks x 8 columns
+        const int blk = tid >> 3, jj = tid & 7, b0 = blk * 8, j = b0 + jj;
+        for (int r = j; r < b0 + 8; ++r) {
             T sum = (r == j) ? T(1) : T(0);
             for (int k = j; k < r; ++k) sum = fma(-s[r][k], x[k][j], sum);
-            x[r][j] = sum / s[r][r];
+            x[r][j] = sum * yv[r];
         }
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int h = 8; h < kTile; h *= 2) {  // block size h -> 2h
+        const int nblk = kTile / (2 * h);
+        // tmp = L21 X11 for every 2h-block (h x h each)
+        for (int e = tid; e < nblk * h * h; e += NT) {
+            const int bi = e / (h * h), rem = e % (h * h), r = rem / h, c = rem % h;
+            const int o = bi * 2 * h;
+            T sum = T(0);
+            for (int k = c; k < h; ++k) sum = fma(s[o + h + r][o + k], x[o + k][o + c], sum);
+            tmp[o + h + r][o + c] = sum;
+        }
+        __syncthreads();
+        // X21 = -X22 tmp
+        for (int e = tid; e < nblk * h * h; e += NT) {
+            const int bi = e / (h * h), rem = e % (h * h), r = rem / h, c = rem % h;
+            const int o = bi * 2 * h;
+            T sum = T(0);
+            for (int k = 0; k <= r; ++k) sum = fma(x[o + h + r][o + h + k], tmp[o + h + k][o + c], sum);
+            x[o + h + r][o + c] = -sum;
+        }
+        __syncthreads();
     }
 }
 
+// Cholesky of one <= 32 x 32 diagonal tile plus its inverse.  Right-looking:
+// per column one warp forms the reciprocal pivot 1/sqrt(d) and scales the
+// column (one multiply per row instead of a division), then all warps apply
+// the rank-1 update to the trailing triangle.
 template <typename T>
 __global__ void __launch_bounds__(NT)
 k_potrf_tile(T* A, int64_t ld, int nb, int zero_right, T* tinv, int32_t* info, int64_t row0) {
     __shared__ T s[kTile][kTile + 1];
     __shared__ T x[kTile][kTile + 1];
+    __shared__ T tmp[kTile][kTile + 1];
+    __shared__ T yv[kTile];
     __shared__ int fail;
     const int tid = threadIdx.x;
 
-    for (int e = tid; e < nb * nb; e += NT) {
-        const int r = e / nb, c = e - (e / nb) * nb;
-        s[r][c] = (c <= r) ? A[(int64_t)r * ld + c] : T(0);
+    for (int e = tid; e < kTile * kTile; e += NT) {
+        const int r = e / kTile, c = e % kTile;
+        T v = T(0);
+        if (r < nb && c <= r) v = A[(int64_t)r * ld + c];
+        else if (r >= nb && r == c) v = T(1);  // identity padding
+        s[r][c] = v;
     }
     if (tid == 0) fail = 0;
+    if (tid < kTile) yv[tid] = T(1);
     __syncthreads();
 
     for (int j = 0; j < nb; ++j) {
-        if (tid == 0) {
-            T d = s[j][j];
-            if (!(d > T(0)) || !isfinite((double)d)) {
-                if (fail == 0) fail = j + 1;
-                d = T(NAN);
+        if (tid < 32) {
+            const T d = s[j][j];
+            const bool bad = !(d > T(0)) || !isfinite((double)d);
+            const T y = bad ? T(NAN) : sgb_rsqrt<T>(d);
+            const int r = tid;
+            if (r > j && r < nb) s[r][j] *= y;
+            if (r == j) {
+                s[j][j] = d * y;
+                yv[j] = y;
+                if (bad && fail == 0) fail = j + 1;
             }
-            s[j][j] = sgb_sqrt(d);
         }
         __syncthreads();
-        const T piv = s[j][j];
         const int rem = nb - j - 1;
-        if (tid < rem) s[j + 1 + tid][j] = s[j + 1 + tid][j] / piv;
-        __syncthreads();
         for (int e = tid; e < rem * rem; e += NT) {
             const int rr = j + 1 + e / rem, cc = j + 1 + (e - (e / rem) * rem);
             if (cc <= rr) s[rr][cc] = fma(-s[rr][j], s[cc][j], s[rr][cc]);
@@ -80,8 +124,7 @@ k_potrf_tile(T* A, int64_t ld, int nb, int zero_right, T* tinv, int32_t* info, i
 
     if (tid == 0 && fail != 0 && info != nullptr) atomicCAS(info, 0, (int32_t)(row0 + fail));
 
-    tile_inverse<T>(s, x, nb);
-    __syncthreads();
+    tile_inverse<T>(s, x, tmp, yv);
 
     for (int e = tid; e < nb * nb; e += NT) {
         const int r = e / nb, c = e - (e / nb) * nb;
@@ -102,17 +145,23 @@ __global__ void __launch_bounds__(NT)
 k_trtri_tiles(const T* L, int64_t ldl, int64_t strideL, int m, T* X, int64_t ldx, int64_t strideX) {
     __shared__ T s[kTile][kTile + 1];
     __shared__ T x[kTile][kTile + 1];
+    __shared__ T tmp[kTile][kTile + 1];
+    __shared__ T yv[kTile];
     const int t0 = blockIdx.x * kTile;
     const int nb = min(kTile, m - t0);
     const T* Lb = L + (int64_t)blockIdx.y * strideL + (int64_t)t0 * ldl + t0;
     T* Xb = X + (int64_t)blockIdx.y * strideX + (int64_t)t0 * ldx + t0;
-    for (int e = threadIdx.x; e < nb * nb; e += NT) {
-        const int r = e / nb, c = e - (e / nb) * nb;
-        s[r][c] = (c <= r) ? Lb[(int64_t)r * ldl + c] : T(0);
+    for (int e = threadIdx.x; e < kTile * kTile; e += NT) {
+        const int r = e / kTile, c = e % kTile;
+        T v = T(0);
+        if (r < nb && c <= r) v = Lb[(int64_t)r * ldl + c];
+        else if (r >= nb && r == c) v = T(1);
+        s[r][c] = v;
     }
     __syncthreads();
-    tile_inverse<T>(s, x, nb);
+    if (threadIdx.x < kTile) yv[threadIdx.x] = T(1) / s[threadIdx.x][threadIdx.x];
     __syncthreads();
+    tile_inverse<T>(s, x, tmp, yv);
     for (int e = threadIdx.x; e < nb * nb; e += NT) {
         const int r = e / nb, c = e - (e / nb) * nb;
         Xb[(int64_t)r * ldx + c] = x[r][c];

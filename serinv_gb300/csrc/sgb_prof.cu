@@ -50,8 +50,13 @@ void recycle_locked() {
 
 }  // namespace
 
+bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
+}
+
 void prof_before(cudaStream_t s) {
-    if (!g_enabled.load(std::memory_order_relaxed)) return;
+    if (!g_enabled.load(std::memory_order_relaxed) || capturing(s)) return;
     std::lock_guard<std::mutex> lk(g_mu);
     t_start = get_event();
     cudaEventRecord(t_start, s);
