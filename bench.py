@@ -48,7 +48,8 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    p.add_argument("--precision", default="fp64",
+                   help="fp64 | mixed | mixed:S (S = slice count 3..7)")
     p.add_argument("--n", type=int, default=512)
     p.add_argument("--b", type=int, default=512)
     p.add_argument("--a", type=int, default=64)

@@ -59,8 +59,10 @@ extern "C" {
  * bf16 slice products (fixed-point split of each FP64 operand into S
  * base-128 digits) accumulated exactly in FP32 TMEM and summed in FP64;
  * diagonal-tile pivots stay in FP64.  S goes in bits 8-15 of the precision
- * argument (3..7; 0 selects 5): SGB_PREC_MIXED | (S << 8).  Normwise
- * product error ~2^-(7S+1): S=5 ~1e-11, S=7 ~1e-15.  FP64 storage only.
+ * argument (3..7; 0 selects 6): SGB_PREC_MIXED | (S << 8).  Per-product
+ * error ~2^-(7S+1) of the row maxima; measured on pobtaf+pobtasi at
+ * n=512, b=512, a=64: S=5 ~4e-9, S=6 ~3e-11, S=7 ~3e-13 relative.
+ * FP64 storage only.
  * The first 4 bytes of the workspace receive a device status word (0, or
  * SGB_ERR_TIMEOUT if a bounded tensor-core wait gave up).                 */
 #define SGB_PREC_MIXED  1

@@ -34,7 +34,7 @@ PRECISIONS = {"native": SGB_PREC_NATIVE, "fp64": SGB_PREC_NATIVE, "mixed": SGB_P
 
 
 def precision_code(precision) -> int:
-    """'fp64' / 'native' -> native; 'mixed' -> 5 slices; 'mixed:S' -> S slices (3..7)."""
+    """'fp64' / 'native' -> native; 'mixed' -> 6 slices; 'mixed:S' -> S slices (3..7)."""
     if isinstance(precision, str) and precision.startswith("mixed:"):
         S = int(precision.split(":", 1)[1])
         if not 3 <= S <= 7:

@@ -18,7 +18,7 @@ loaded or no GPU is present, the call raises — there is no CPU fallback.
 Extensions (keyword-only, absent from the reference): ``precision`` —
 ``"fp64"`` (default, arithmetic in the storage type), ``"mixed"`` (FP64
 storage, block products as exact bf16 slice products on the tensor cores,
-5 slices) or ``"mixed:S"`` (S slices, 3..7; S=7 is FP64-accurate);
+6 slices) or ``"mixed:S"`` (S slices, 3..7; S=7 is FP64-accurate);
 ``check_spd`` (pobtaf, default True) — synchronise and raise
 ``numpy.linalg.LinAlgError`` on a non-positive pivot, like SciPy's
 ``cholesky`` in the reference.

@@ -40,7 +40,7 @@ int check_bta(const sgb_bta* m) {
 // precision: SGB_PREC_NATIVE, or SGB_PREC_MIXED with the slice count in
 // bits 8-15 (0 = default kDefaultSlices).  Returns the slice count (0 for
 // native) or a negative error code.
-constexpr int kDefaultSlices = 5;
+constexpr int kDefaultSlices = 6;
 
 int parse_precision(int precision, int dtype) {
     const int mode = precision & 0xff;
@@ -61,6 +61,13 @@ struct Ctx {
     size_t tc_bytes = 0;
     int32_t* status = nullptr;  // device status word (SGB_ERR_TIMEOUT on a stuck wait)
 };
+
+// Mixed pobtaf: factor [D_i; Lo_i; Ar_i] with the tall-panel sweep (false),
+// or factor D_i alone, invert it and run the TRSMs on the tensor cores
+// (true).  The second moves the TRSM flops to the tensor cores but needs a
+// triangular inversion per block (two dozen small launches), which costs
+// more than it saves at b = 512 on the launch-bound diagonal chain.
+constexpr bool kMixedInverseTrsm = false;
 
 // Upper bound of the tensor-core scratch of one grouped launch with up to
 // `nprob` problems whose sizes are at most mx x mx and K at most kmax.
@@ -97,6 +104,37 @@ cudaError_t run_gemm<double>(const Ctx& c, GemmProb<double>* pr, int np, cudaStr
     return cudaSuccess;
 }
 
+template <typename T>
+cudaError_t ctx_gemm(void* c, GemmProb<T>* pr, int np, cudaStream_t s) {
+    return run_gemm<T>(*(const Ctx*)c, pr, np, s);
+}
+
+// Tensor-core scratch of one row-sweep product of a batched triangular
+// inversion of `batch` m x m blocks (32-row strips: M = 32, N, K <= m).
+size_t trtri_tc_bytes(int S, int64_t m, int64_t batch) {
+    const int64_t Npad = ceil_div(m, kTcBN) * kTcBN, Kpad = ceil_div(m, 32) * 32;
+    const size_t per = (size_t)S * (128 + Npad) * Kpad * 2 + (size_t)(128 + Npad) * 4;
+    return (size_t)batch * ((per + 255) / 256 * 256) + 512;
+}
+
+// Matrices per chunk of a tensor-core batched inversion (bounds the scratch).
+constexpr int64_t kTrtriChunk = 64;
+
+// Batched L^{-1}: SIMT products natively, tensor-core products in mixed
+// mode (in chunks of kTrtriChunk blocks so the slice scratch stays bounded).
+template <typename T>
+cudaError_t trtri_run(const Ctx& cx, const T* L, int64_t m, int64_t batch, T* Linv, T* scratch, cudaStream_t s) {
+    const int64_t mm = m * m;
+    if (cx.slices == 0 || m <= kTile) return trtri_batched<T>(L, m, mm, m, batch, Linv, m, mm, scratch, s);
+    for (int64_t j0 = 0; j0 < batch; j0 += kTrtriChunk) {
+        const int64_t nb = (batch - j0) < kTrtriChunk ? (batch - j0) : kTrtriChunk;
+        cudaError_t e = trtri_batched<T>(L + j0 * mm, m, mm, m, nb, Linv + j0 * mm, m, mm, scratch, s,
+                                         ctx_gemm<T>, (void*)&cx);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 // ---- workspace layouts ------------------------------------------------
 
 struct Carve {
@@ -116,7 +154,11 @@ struct PobtafWs {
         status = c.take(256);
         tinv = c.take(sizeof(T) * kTile * kTile);
         const int64_t mx = m->b > m->a ? m->b : m->a;
-        tc_bytes = S ? tc_bound(S, mx, m->b, 3) : 0;
+        tc_bytes = 0;
+        if (S) {
+            const size_t g = tc_bound(S, mx, m->b, 3), t1 = trtri_tc_bytes(S, m->b, 1);
+            tc_bytes = g > t1 ? g : t1;
+        }
         tc = c.take(tc_bytes);
         // mixed precision only: L_ii^{-1} and its triangular-inverse scratch
         linv = c.take(S ? sizeof(T) * m->b * m->b : 0);
@@ -133,7 +175,14 @@ struct PobtasiWs {
         const size_t mx = b > a ? b : a;
         Carve c;
         status = c.take(256);
-        tc_bytes = S ? tc_bound(S, (int64_t)mx, (int64_t)(b + a), 3) : 0;
+        tc_bytes = 0;
+        if (S) {
+            const size_t g = tc_bound(S, (int64_t)mx, (int64_t)(b + a), 3);
+            const int64_t chunk = (int64_t)n < kTrtriChunk ? (int64_t)n : kTrtriChunk;
+            const size_t t1 = trtri_tc_bytes(S, (int64_t)b, chunk), t2 = trtri_tc_bytes(S, (int64_t)a, 1);
+            tc_bytes = g > t1 ? g : t1;
+            tc_bytes = tc_bytes > t2 ? tc_bytes : t2;
+        }
         tc = c.take(tc_bytes);
         linv = c.take(sizeof(T) * n * b * b);
         linv_tip = c.take(sizeof(T) * a * a);
@@ -233,13 +282,13 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
     // is formed and the TRSMs run as tensor-core products with L_ii^{-T}.
     auto factor = [&](int64_t i, RowSet<T> r1, RowSet<T> r2) -> int {
         T* Di = D + i * bb;
-        if (S == 0) {
+        if (S == 0 || !kMixedInverseTrsm) {
             cudaError_t e = factor_column_block<T>(Di, b, b, r1, r2, tinv, info, i * b, s);
             return e == cudaSuccess ? SGB_OK : cuda_fail(e);
         }
         RowSet<T> none{nullptr, 0, b};
         cudaError_t e = factor_column_block<T>(Di, b, b, none, none, tinv, info, i * b, s);
-        if (e == cudaSuccess) e = trtri_batched<T>(Di, b, bb, b, 1, Linv, b, bb, trs, s);
+        if (e == cudaSuccess) e = trtri_run<T>(cx, Di, b, 1, Linv, trs, s);
         if (e != cudaSuccess) return cuda_fail(e);
         GemmProb<T> pr[2];
         int np = 0;
@@ -355,11 +404,11 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
     const int64_t bb = b * b, ab = a * b;
 
     const int64_t ninv = invert_last_block ? n : n - 1;
-    SGB_TRY(trtri_batched<T>(D, b, bb, b, ninv, Linv, b, bb, trs, s));
+    SGB_TRY(trtri_run<T>(cx, D, b, ninv, Linv, trs, s));
 
     if (invert_last_block && a) {
         // X_T = L_T^{-T} L_T^{-1}  (:115-119)
-        SGB_TRY(trtri_batched<T>(Tp, a, a * a, a, 1, Ltinv, a, a * a, trs, s));
+        SGB_TRY(trtri_run<T>(cx, Tp, a, 1, Ltinv, trs, s));
         GemmProb<T> p = prob<T>();
         p.M = p.N = (int32_t)a;
         set_term<T>(p, 0, Ltinv, a, 1, Ltinv, a, 0, a, KM_GE_M0);

@@ -97,11 +97,19 @@ template <typename T>
 cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, RowSet<T> r2,
                                 T* scratch, int32_t* info, int64_t info_row0, cudaStream_t s);
 
+// A grouped-product engine: the SIMT kernel, or a context-bound dispatcher
+// that sends products to the tensor cores.
+template <typename T>
+using GemmFn = cudaError_t (*)(void* ctx, GemmProb<T>* probs, int np, cudaStream_t s);
+
 // Full triangular inverse of `batch` lower-triangular m x m blocks:
 // Linv_j = L_j^{-1} (zeros above the diagonal).  Scratch: batch*kTile*m T.
+// The row-sweep products go through `fn(fnctx, ...)` when given, else the
+// SIMT kernel.
 template <typename T>
 cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, int64_t batch,
-                          T* Linv, int64_t ldx, int64_t strideX, T* scratch, cudaStream_t s);
+                          T* Linv, int64_t ldx, int64_t strideX, T* scratch, cudaStream_t s,
+                          GemmFn<T> fn = nullptr, void* fnctx = nullptr);
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

@@ -75,10 +75,14 @@ __device__ __forceinline__ void tile_inverse(T (*s)[kTile + 1], T (*x)[kTile + 1
     }
 }
 
-// Cholesky of one <= 32 x 32 diagonal tile plus its inverse.  Right-looking:
-// per column one warp forms the reciprocal pivot 1/sqrt(d) and scales the
-// column (one multiply per row instead of a division), then all warps apply
-// the rank-1 update to the trailing triangle.
+// Cholesky of one <= 32 x 32 diagonal tile plus its inverse, with a
+// one-column lookahead.  Warp 0 (alone on its SM quarter, so nothing else
+// competes for that quarter's FP64 unit) owns the pivot chain: per column j
+// it forms 1/sqrt(d_j), scales column j, and after the barrier applies
+// column j to column j+1 only, so the next pivot is ready.  Warps on the
+// other three quarters (1-3, 5-7) meanwhile apply column j-1 to columns
+// j+1.. of the trailing triangle.  One barrier per column; the dependent
+// FP64 chain per column is rsqrt + one multiply + one FMA.
 template <typename T>
 __global__ void __launch_bounds__(NT)
 k_potrf_tile(T* A, int64_t ld, int nb, int zero_right, T* tinv, int32_t* info, int64_t row0) {
@@ -87,7 +91,7 @@ k_potrf_tile(T* A, int64_t ld, int nb, int zero_right, T* tinv, int32_t* info, i
     __shared__ T tmp[kTile][kTile + 1];
     __shared__ T yv[kTile];
     __shared__ int fail;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     for (int e = tid; e < kTile * kTile; e += NT) {
         const int r = e / kTile, c = e % kTile;
@@ -100,27 +104,37 @@ k_potrf_tile(T* A, int64_t ld, int nb, int zero_right, T* tinv, int32_t* info, i
     if (tid < kTile) yv[tid] = T(1);
     __syncthreads();
 
+    // update workers: warps 1,2,3,5,6,7 -> worker index 0..5
+    const int wk = warp == 0 || warp == 4 ? -1 : (warp < 4 ? warp - 1 : warp - 2);
+    const int nworkers = 6 * 32;
     for (int j = 0; j < nb; ++j) {
-        if (tid < 32) {
+        if (warp == 0) {
             const T d = s[j][j];
             const bool bad = !(d > T(0)) || !isfinite((double)d);
             const T y = bad ? T(NAN) : sgb_rsqrt<T>(d);
-            const int r = tid;
+            const int r = lane;
             if (r > j && r < nb) s[r][j] *= y;
             if (r == j) {
                 s[j][j] = d * y;
                 yv[j] = y;
                 if (bad && fail == 0) fail = j + 1;
             }
+        } else if (wk >= 0 && j >= 1) {
+            // column j-1 applied to columns j+1 .. nb-1 (column j was done by warp 0)
+            const int c0 = j + 1, k = j - 1;
+            const int w = nb - c0;  // trailing width
+            for (int e = wk * 32 + lane; e < w * w; e += nworkers) {
+                const int rr = c0 + e / w, cc = c0 + e % w;
+                if (cc <= rr) s[rr][cc] = fma(-s[rr][k], s[cc][k], s[rr][cc]);
+            }
         }
         __syncthreads();
-        const int rem = nb - j - 1;
-        for (int e = tid; e < rem * rem; e += NT) {
-            const int rr = j + 1 + e / rem, cc = j + 1 + (e - (e / rem) * rem);
-            if (cc <= rr) s[rr][cc] = fma(-s[rr][j], s[cc][j], s[rr][cc]);
+        if (warp == 0 && j + 1 < nb) {  // lookahead: column j applied to column j+1
+            const int r = lane;
+            if (r >= j + 1 && r < nb) s[r][j + 1] = fma(-s[r][j], s[j + 1][j], s[r][j + 1]);
         }
-        __syncthreads();
     }
+    __syncthreads();
 
     if (tid == 0 && fail != 0 && info != nullptr) atomicCAS(info, 0, (int32_t)(row0 + fail));
 
@@ -275,7 +289,8 @@ cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, R
 
 template <typename T>
 cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, int64_t batch, T* Linv,
-                          int64_t ldx, int64_t strideX, T* scratch, cudaStream_t s) {
+                          int64_t ldx, int64_t strideX, T* scratch, cudaStream_t s, GemmFn<T> fn, void* fnctx) {
+    auto gemm = [&](GemmProb<T>* p) { return fn ? fn(fnctx, p, 1, s) : gemm_simt<T>(p, 1, s); };
     if (m <= 0 || batch <= 0) return cudaSuccess;
     cudaError_t err;
     // Zero the strict upper triangle (and everything else) first; the row
@@ -308,7 +323,7 @@ cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, i
         p.Cout = scratch;
         p.ldc = m;
         p.strideC = (int64_t)kTile * m;
-        err = gemm_simt<T>(&p, 1, s);
+        err = gemm(&p);
         if (err != cudaSuccess) return err;
         // Linv[r0:r0+rows, 0:r0] = -Linv[r0:, r0:](tile) * tmp
         GemmProb<T> q = blank_prob<T>();
@@ -328,7 +343,7 @@ cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, i
         q.Cout = Linv + r0 * ldx;
         q.ldc = ldx;
         q.strideC = strideX;
-        err = gemm_simt<T>(&q, 1, s);
+        err = gemm(&q);
         if (err != cudaSuccess) return err;
     }
     return cudaSuccess;
@@ -341,7 +356,7 @@ cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, i
     template cudaError_t factor_column_block<T>(T*, int64_t, int64_t, RowSet<T>, RowSet<T>, T*,          \
                                                 int32_t*, int64_t, cudaStream_t);                         \
     template cudaError_t trtri_batched<T>(const T*, int64_t, int64_t, int64_t, int64_t, T*, int64_t,     \
-                                          int64_t, T*, cudaStream_t);
+                                          int64_t, T*, cudaStream_t, GemmFn<T>, void*);
 SGB_INST(double)
 SGB_INST(float)
 
