@@ -1,5 +1,6 @@
 #!/usr/bin/env python
-"""Benchmark: pobtaf + pobtasi throughput on one GB300 (TFLOP/s, matrices/s).
+"""Benchmark: pobtaf + pobtasi throughput on one GB300 (TFLOP/s, matrices/s),
+mixed precision against the FP64 form, at the stated relative error.
 
 Workload (default): one SPD block-tridiagonal-with-arrowhead matrix, n=512
 diagonal blocks of size b=512, arrowhead width a=64, float64, generated with
@@ -10,7 +11,11 @@ for a dataset (the reference publishes none).
 One step = restore the input stacks (device-to-device copy) + pobtaf +
 pobtasi, in place.  The inputs (2.28 GB) are larger than L2 (129 MB), so no
 L2 flush is needed between steps.  `value` is canonical TFLOP/s (LAPACK
-flop conventions) over the timed K steps, with device-resident inputs.
+flop conventions) over the timed K steps, with device-resident inputs, for
+the headline form (`--precision`, default "mixed": FP64 storage, block
+products as exact bf16 slice products on the tensor cores, 6 slices); the
+FP64 drop-in is timed beside it (`compare`) and the mixed result's relative
+error against the FP64 result is stated (`rel_err`).
 `e2e` runs the same two calls through the public API on pinned NumPy host
 arrays, host<->device copies included.
 
@@ -48,8 +53,10 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--precision", default="fp64",
-                   help="fp64 | mixed | mixed:S (S = slice count 3..7)")
+    p.add_argument("--precision", default="mixed",
+                   help="fp64 | mixed | mixed:S (S = slice count 3..7); the headline form")
+    p.add_argument("--compare", default="fp64",
+                   help="comma-separated forms timed beside the headline (empty: none)")
     p.add_argument("--n", type=int, default=512)
     p.add_argument("--b", type=int, default=512)
     p.add_argument("--a", type=int, default=64)
@@ -58,6 +65,11 @@ def parse():
     p.add_argument("--cpu-sample-blocks", type=int, default=32)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", choices=["bta", "batched", "kappa", "autograd"], default="bta")
+    p.add_argument("--batch-count", type=int, default=256)
+    p.add_argument("--batch-precision", choices=["native", "mixed"], default="native")
+    p.add_argument("--ag-n", type=int, default=1024)
+    p.add_argument("--ag-fd", type=int, default=64)
     return p.parse_args()
 
 
@@ -190,6 +202,71 @@ def bench_reference(args, rank: int, world: int):
 
 # ---------------------------------------------------------------- our arm
 
+def _timed_sweeps(torch, sg, _lib, A, A0, prec, steps, warmup, local, dist):
+    """W warm-up + K timed steps (restore, pobtaf, pobtasi) with clocks and kernel profile."""
+    def step():
+        for x, y in zip(A, A0):
+            x.copy_(y)
+        sg.pobtaf(*A, precision=prec, check_spd=False)
+        sg.pobtasi(*A, precision=prec)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = _lib.launch_count()
+    _lib.profile_enable(True)
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    launches = _lib.launch_count() - launches0
+    prof = _lib.profile_read()
+    _lib.profile_enable(False)
+    clk = clocks.stop()
+    if dist is not None:
+        t = torch.tensor([elapsed], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    return elapsed / steps, launches, prof, clk
+
+
+def _roofline(torch, prof):
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else (None, None)
+    if dom[0] is None:
+        return None
+    peaks = measured_peaks()
+    k, d = dom
+    achieved = d["flops"] / (d["ms"] / 1e3) / 1e12
+    if k == "gemm_tc":
+        peak, src = peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (of measured)"
+    else:
+        peak, src = fp64_peak_live(torch), "cuBLAS DGEMM 4096^3 measured live (of measured)"
+    return {"bound": "tensor" if k == "gemm_tc" else "fp64-pipe", "kernel": k,
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": src, "traffic": None,
+            "avg_launch_ms": d["ms"] / d["launches"],
+            "share_of_device_time": d["ms"] / sum(v["ms"] for v in prof.values())}
+
+
+def _dtype_label(prec: str) -> str:
+    if prec.startswith("mixed"):
+        S = int(prec.split(":")[1]) if ":" in prec else 6
+        return f"f64 storage, products as {S} exact bf16 slices (tcgen05, fp32 accumulate)"
+    return "f64"
+
+
 def bench_ours(args, rank: int, world: int, dist):
     import torch
 
@@ -208,73 +285,34 @@ def bench_ours(args, rank: int, world: int, dist):
     A = [x.clone() for x in A0]
     prec = args.precision
 
-    def step():
-        for x, y in zip(A, A0):
-            x.copy_(y)
-        sg.pobtaf(*A, precision=prec, check_spd=False)
-        sg.pobtasi(*A, precision=prec)
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
-    launches0 = _lib.launch_count()
-    _lib.profile_enable(True)
-    stream = torch.cuda.current_stream()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        step()
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    if dist is not None:
-        dist.barrier()
-    elapsed = ev0.elapsed_time(ev1) / 1e3
-    launches = _lib.launch_count() - launches0
-    prof = _lib.profile_read()
-    _lib.profile_enable(False)
-    clk = clocks.stop()
-
-    if dist is not None:
-        t = torch.tensor([elapsed], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-    per_step = elapsed / args.steps
+    per_step, launches, prof, clk = _timed_sweeps(torch, sg, _lib, A, A0, prec, args.steps, args.warmup,
+                                                  local, dist)
     value = step_flops * world / per_step / 1e12
 
-    # accuracy statement: mixed is compared against this GPU's FP64 path
+    # the comparison forms (e.g. the FP64 drop-in beside the mixed form)
+    compare = {}
+    for cp in [c for c in args.compare.split(",") if c and c != prec]:
+        Ac = [x.clone() for x in A0]
+        ps, _, pr, _ = _timed_sweeps(torch, sg, _lib, Ac, A0, cp, max(1, args.steps // 2), 1, local, dist)
+        compare[cp] = {"value": step_flops * world / ps / 1e12, "unit": "TFLOP/s", "ms_per_step": ps * 1e3,
+                       "kernel_profile_ms": {k: round(v["ms"], 2) for k, v in pr.items()}}
+        del Ac
+
+    # accuracy statement: a mixed form is compared with this GPU's FP64 path
+    # (which the test suite pins to the reference at <= 1e-12)
     acc = {}
-    if prec == "mixed":
+    if prec.startswith("mixed"):
         ref = [x.clone() for x in A0]
         sg.pobtaf(*ref)
         sg.pobtasi(*ref)
         for name, x, y in zip(("diag", "lower", "arrow", "tip"), A, ref):
             acc[name] = float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
+        acc["vs"] = "FP64 drop-in on the same inputs (relative Frobenius error per stack)"
+        del ref
     else:
         acc = {"note": "FP64 path; parity with the reference pinned at <=1e-12 by the test suite"}
 
-    # roofline for the dominant kernel class
-    dom = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else (None, None)
-    peaks = measured_peaks()
-    roof = None
-    if dom[0] is not None:
-        k, d = dom
-        achieved = d["flops"] / (d["ms"] / 1e3) / 1e12
-        if k == "gemm_tc":
-            peak, src = peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (of measured)"
-        else:
-            peak, src = fp64_peak_live(torch), "cuBLAS DGEMM 4096^3 measured live (of measured)"
-        roof = {"bound": "tensor" if k == "gemm_tc" else "fp64-pipe", "kernel": k,
-                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "peak_source": src, "traffic": None,
-                "avg_launch_ms": d["ms"] / d["launches"],
-                "share_of_device_time": d["ms"] / sum(v["ms"] for v in prof.values())}
+    roof = _roofline(torch, prof)
 
     # end to end through the public API with pinned host arrays
     e2e = None
@@ -311,13 +349,14 @@ def bench_ours(args, rank: int, world: int, dist):
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
+            "dtype": _dtype_label(prec), "data": "synthetic (seeded generator, seed 0)",
             "config": {"workload": f"BTA n={n} b={b} a={a} float64, pobtaf+pobtasi",
                        "n": n, "b": b, "a": a, "precision": prec,
                        "l2": "inputs larger than L2 (2.28 GB), no flush",
                        "parallelism": f"replicas x{world}"},
             "matrices_per_s": world / per_step,
             "rel_err": acc,
+            "compare": compare,
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -329,12 +368,196 @@ def bench_ours(args, rank: int, world: int, dist):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- other workloads
+
+def bench_batched(args):
+    """256 uneven matrices (n ~ U{16..256}, b in {32,64,128,256}, a in {0,4,16}),
+    half float32 / half float64, 4 RHS each, in one graph launch per step:
+    pobtaf -> pobtas N/T -> pobtasi for every matrix.  Stream count from the
+    autotuner.  Value: matrices/s."""
+    import torch
+
+    from serinv_gb300 import _lib
+    from serinv_gb300.batched import BatchPlan, autotune_nstreams
+    from serinv_gb300.synthetic import generate_torch
+
+    torch.cuda.set_device(0)
+    _lib.load()
+    rng = np.random.default_rng(0)
+    count = args.batch_count
+    shapes = []
+    for i in range(count):
+        n = int(rng.integers(16, 257))
+        b = int(rng.choice([32, 64, 128, 256]))
+        a = int(rng.choice([0, 4, 16]))
+        dt = torch.float32 if i < count // 2 else torch.float64
+        shapes.append((n, b, a, dt))
+    src, rhs0 = [], []
+    tot_flops = 0.0
+    for i, (n, b, a, dt) in enumerate(shapes):
+        D, Lo, Ar, T, B = generate_torch(n, b, a, 4, seed=i, dtype=dt)
+        src.append((D, Lo, Ar, T))
+        rhs0.append(B)
+        f = flops(n, b, a, 4)
+        tot_flops += f["pobtaf"] + f["pobtasi"] + f["pobtas"]
+    work = [tuple(x.clone() for x in m) for m in src]
+    rhs = [r.clone() for r in rhs0]
+    prec = ["mixed" if args.batch_precision == "mixed" else "fp64"] * count
+    t0 = time.perf_counter()
+    ns = autotune_nstreams(work, rhs, precisions=prec, candidates=(8, 16, 32, 64), reps=1)
+    tune_s = time.perf_counter() - t0
+    plan = BatchPlan(work, rhs, precisions=prec, nstreams=ns)
+
+    def restore():
+        for d, s_ in zip(work, src):
+            for x, y in zip(d, s_):
+                x.copy_(y)
+        for d, s_ in zip(rhs, rhs0):
+            d.copy_(s_)
+
+    for _ in range(args.warmup):
+        restore()
+        plan.run()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        restore()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        plan.run()
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = float(np.median(times))
+    bad = int((plan.info() != 0).sum())
+    line = {"metric": "batched BTA matrices/s (256 uneven, f32+f64, pobtaf+pobtas+pobtasi, 1 graph launch)",
+            "value": count / t, "unit": "matrices/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "tflops": tot_flops / t / 1e12,
+            "dtype": "half f32, half " + ("f64 mixed" if args.batch_precision == "mixed" else "f64"),
+            "data": "synthetic (torch generator, seed i for matrix i)",
+            "config": {"workload": "batch of 256 uneven BTA matrices", "nstreams": ns,
+                       "autotune_s": tune_s, "not_spd": bad}}
+    print(json.dumps(line), flush=True)
+
+
+def bench_kappa(args):
+    """Mixed vs FP64 at targeted condition numbers (kappa in 1e2, 1e5, 1e8):
+    A = A0 + sigma I with sigma from Lanczos extremes of A0; the achieved
+    kappa is measured (lambda_min through the FP64 factor)."""
+    import torch
+
+    import serinv_gb300 as sg
+    from serinv_gb300 import _lib
+    from serinv_gb300.conditioning import bta_matvec, kappa_of, lanczos_extremes, shift_for_kappa
+    from serinv_gb300.synthetic import generate_torch
+
+    torch.cuda.set_device(0)
+    _lib.load()
+    n, b, a = args.n, args.b, args.a
+    D0, Lo, Ar, T0, _ = generate_torch(n, b, a, 1, seed=0, shift=0.0)
+    N = n * b + a
+    lmin0, lmax0 = lanczos_extremes(lambda v: bta_matvec(D0, Lo, Ar, T0, v), N, steps=120)
+    out = []
+    f = flops(n, b, a)
+    for kappa in (1e2, 1e5, 1e8):
+        sigma = shift_for_kappa(lmin0, lmax0, kappa)
+        idx = torch.arange(b, device="cuda")
+        D = D0.clone()
+        D[:, idx, idx] += sigma
+        T = T0.clone()
+        if a:
+            ti = torch.arange(a, device="cuda")
+            T[ti, ti] += sigma
+        achieved, lmin, lmax = kappa_of(D, Lo, Ar, T)
+        res = {"kappa_target": kappa, "kappa_achieved": achieved, "sigma": sigma}
+        ref = [x.clone() for x in (D, Lo, Ar, T)]
+        sg.pobtaf(*ref)
+        sg.pobtasi(*ref)
+        for prec in [p for p in args.compare.split(",") if p] + [args.precision]:
+            if prec == "fp64":
+                continue
+            X = [x.clone() for x in (D, Lo, Ar, T)]
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            sg.pobtaf(*X, precision=prec, check_spd=False)
+            sg.pobtasi(*X, precision=prec)
+            e1.record()
+            e1.synchronize()
+            dt = e0.elapsed_time(e1) / 1e3
+            res[prec] = {"tflops": (f["pobtaf"] + f["pobtasi"]) / dt / 1e12,
+                         "rel_err": {nm: float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
+                                     for nm, x, y in zip(("diag", "lower", "arrow", "tip"), X, ref)}}
+        out.append(res)
+        del ref
+    line = {"metric": "mixed-precision error vs conditioning (pobtaf+pobtasi against FP64)",
+            "config": {"n": n, "b": b, "a": a, "lanczos_A0": [lmin0, lmax0]}, "results": out}
+    print(json.dumps(line), flush=True)
+
+
+def bench_autograd(args):
+    """logdet(A) + y^T A^{-1} y with its selected-inversion backward at
+    n=1024, b=256, a=32 (FP64): forward+backward time, central finite
+    differences (h=1e-6) on 64 seeded entries, and dense torch autograd at n=16."""
+    import torch
+
+    from serinv_gb300 import _lib
+    from serinv_gb300.autograd import bta_logdet_quad
+    from serinv_gb300.synthetic import generate_torch
+
+    torch.cuda.set_device(0)
+    _lib.load()
+    n, b, a = args.ag_n, 256, 32
+    D, Lo, Ar, T, y = generate_torch(n, b, a, 1, seed=0)
+    params = [x.clone().requires_grad_(True) for x in (D, Lo, Ar, T)]
+    yy = y[:, 0].clone().requires_grad_(True)
+    for _ in range(2):
+        for p in params + [yy]:
+            p.grad = None
+        bta_logdet_quad(*params, yy).backward()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        for p in params + [yy]:
+            p.grad = None
+        loss = bta_logdet_quad(*params, yy)
+        loss.backward()
+    torch.cuda.synchronize()
+    t_fb = (time.perf_counter() - t0) / reps
+    rng = np.random.default_rng(0)
+    h = 1e-6
+    worst = 0.0
+    for _ in range(args.ag_fd):
+        w = int(rng.integers(0, 4))
+        t = params[w]
+        idx = tuple(int(rng.integers(0, s_)) for s_ in t.shape)
+        if w in (0, 3) and idx[-1] > idx[-2]:
+            idx = idx[:-2] + (idx[-1], idx[-2])
+        with torch.no_grad():
+            pl = [x.detach().clone() for x in params]
+            mi = [x.detach().clone() for x in params]
+            pl[w][idx] += h
+            mi[w][idx] -= h
+            fd = (float(bta_logdet_quad(*pl, yy.detach())) - float(bta_logdet_quad(*mi, yy.detach()))) / (2 * h)
+        g = float(t.grad[idx])
+        worst = max(worst, abs(fd - g) / max(1.0, abs(g)))
+    line = {"metric": "logdet+quadratic-form forward+backward time (selected-inversion backward)",
+            "value": t_fb * 1e3, "unit": "ms", "higher_is_better": False,
+            "config": {"n": n, "b": b, "a": a, "dtype": "f64"},
+            "finite_difference": {"entries": args.ag_fd, "h": h, "max_rel_dev": worst}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         bench_reference(args, rank, world)
+        return
+    if args.workload != "bta":
+        {"batched": bench_batched, "kappa": bench_kappa, "autograd": bench_autograd}[args.workload](args)
         return
     dist = None
     if world > 1:

@@ -128,3 +128,51 @@ def flops(n: int, b: int, a: int, nrhs: int = 0) -> dict:
 def nbytes_sweep(n: int, b: int, a: int, itemsize: int = 8) -> float:
     """Algorithmic bytes of one sweep: every stored block read once and written once."""
     return 2.0 * itemsize * (n * b * b + max(n - 1, 0) * b * b + n * a * b + a * a)
+
+
+def generate_torch(n: int, b: int, a: int, nrhs: int = 1, seed: int = 0, dtype=None, device="cuda",
+                   shift: str | float = "dd"):
+    """The same construction as ``generate`` drawn with torch's generator on the GPU.
+
+    Same draw order, distributions and dominance shift; different random
+    numbers (torch's Philox stream, not NumPy's PCG64).  Used where the
+    inputs are too large to draw on the host in reasonable time; parity
+    tests use ``generate``.  Returns (D, Lo, Ar, T, B) torch tensors.
+    """
+    import torch
+
+    dtype = dtype or torch.float64
+    g = torch.Generator(device=device).manual_seed(seed)
+
+    def u(*shape):
+        return torch.rand(shape, generator=g, device=device, dtype=torch.float64) * 2.0 - 1.0
+
+    R = u(n, b, b)
+    Lo = u(n - 1, b, b)
+    Ar = u(n, a, b)
+    S = u(a, a)
+    B = u(n * b + a, nrhs)
+    D = R + R.transpose(1, 2)
+    del R
+    T = S + S.T
+    idx = torch.arange(b, device=device)
+    if isinstance(shift, str):
+        rows = D.abs().sum(dim=2) - torch.diagonal(D, dim1=1, dim2=2).abs()
+        if n > 1:
+            absLo = Lo.abs()
+            rows[1:] += absLo.sum(dim=2)
+            rows[:-1] += absLo.sum(dim=1)
+        if a:
+            absAr = Ar.abs()
+            rows += absAr.sum(dim=1)
+            tip_rows = T.abs().sum(dim=1) - torch.diagonal(T).abs() + absAr.sum(dim=(0, 2))
+        D[:, idx, idx] += 1.0 + rows
+        if a:
+            ti = torch.arange(a, device=device)
+            T[ti, ti] += 1.0 + tip_rows
+    else:
+        D[:, idx, idx] += float(shift)
+        if a:
+            ti = torch.arange(a, device=device)
+            T[ti, ti] += float(shift)
+    return tuple(x.to(dtype).contiguous() for x in (D, Lo, Ar, T, B))
