@@ -208,7 +208,8 @@ int sgb_batch_plan_destroy(sgb_batch_plan* plan);
 #define SGB_KCLASS_TRTRI_TILE  2  /* diagonal-tile triangular inverses         */
 #define SGB_KCLASS_GEMM_TC     3  /* tensor-core (tcgen05) block products      */
 #define SGB_KCLASS_SPLIT       4  /* operand slicing for the tensor-core path  */
-#define SGB_KCLASS_COUNT       5
+#define SGB_KCLASS_PANEL       5  /* persistent column-block Cholesky          */
+#define SGB_KCLASS_COUNT       6
 
 /* Number of kernels this library has launched since it was loaded. */
 long long sgb_launch_count(void);

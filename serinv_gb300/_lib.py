@@ -103,7 +103,7 @@ _SIGNATURES = {
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 
-KCLASS = {"gemm": 0, "potrf_tile": 1, "trtri_tile": 2, "gemm_tc": 3, "split": 4}
+KCLASS = {"gemm": 0, "potrf_tile": 1, "trtri_tile": 2, "gemm_tc": 3, "split": 4, "panel": 5}
 
 _lock = threading.Lock()
 _lib = None

@@ -142,9 +142,9 @@ def _workspace(nbytes: int, device) -> torch.Tensor:
     return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)
 
 
-def _check_status(ws: torch.Tensor, precision: int, what: str) -> None:
-    """Mixed precision: the workspace's first int32 is the device status word."""
-    if (precision & 0xFF) != _lib.SGB_PREC_MIXED:
+def _check_status(ws: torch.Tensor, precision: int, what: str, always: bool = False) -> None:
+    """The workspace's first int32 is the device status word (bounded waits)."""
+    if not always and (precision & 0xFF) != _lib.SGB_PREC_MIXED:
         return
     code = int(ws[:4].view(torch.int32).item())
     _lib.raise_for(code, what)
@@ -205,7 +205,7 @@ def pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_a
                             nbytes.value, info.data_ptr(), _stream(device))
         _lib.raise_for(rc, "pobtaf")
         _finish(w)
-        _check_status(ws, precision, "pobtaf")
+        _check_status(ws, precision, "pobtaf", always=check)
         if check:
             k = int(info.item())
             if k > 0:

@@ -148,10 +148,11 @@ struct Carve {
 
 template <typename T>
 struct PobtafWs {
-    size_t status, tinv, tc, tc_bytes, linv, trtri, total;
+    size_t status, bar, tinv, tc, tc_bytes, linv, trtri, total;
     PobtafWs(const sgb_bta* m, int S = 0) {
         Carve c;
         status = c.take(256);
+        bar = c.take(256);
         tinv = c.take(sizeof(T) * kTile * kTile);
         const int64_t mx = m->b > m->a ? m->b : m->a;
         tc_bytes = 0;
@@ -280,10 +281,18 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
     // sweep over the tall column block (the TRSMs fold into the rank-32
     // updates).  Mixed: only D_i is factored on the FP64 pipe; its inverse
     // is formed and the TRSMs run as tensor-core products with L_ii^{-T}.
+    unsigned* bar = (unsigned*)((char*)ws + L.bar);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    SGB_TRY(cudaStreamIsCapturing(s, &cap));
+    // one cooperative launch per block, except under stream capture (graph
+    // plans) and for small blocks, where the launch-based sweep is used
+    const bool persistent = cap == cudaStreamCaptureStatusNone && b > 2 * kTile;
     auto factor = [&](int64_t i, RowSet<T> r1, RowSet<T> r2) -> int {
         T* Di = D + i * bb;
         if (S == 0 || !kMixedInverseTrsm) {
-            cudaError_t e = factor_column_block<T>(Di, b, b, r1, r2, tinv, info, i * b, s);
+            cudaError_t e = persistent
+                                ? factor_panel_persistent<T>(Di, b, b, r1, r2, tinv, bar, cx.status, info, i * b, s)
+                                : factor_column_block<T>(Di, b, b, r1, r2, tinv, info, i * b, s);
             return e == cudaSuccess ? SGB_OK : cuda_fail(e);
         }
         RowSet<T> none{nullptr, 0, b};

@@ -25,15 +25,20 @@
 // Oishi, Rump) specialised to fixed-point digits and level-grouped exact
 // tensor-core accumulation.
 //
-// Kernel structure (one CTA = one 128 x BN output tile, 128 threads):
-//   * operand slices are staged in shared memory in the no-swizzle K-major
-//     core-matrix layout (8 rows x 16 bytes per core matrix) by cp.async,
-//     two stages;
-//   * thread 0 issues tcgen05.mma (cta_group::1, kind::f16, bf16 inputs,
-//     FP32 accumulation in TMEM) and tcgen05.commit to an mbarrier per stage;
-//   * all mbarrier waits are bounded; on timeout an error word is set and the
-//     kernel drains (bounded) and frees its TMEM before returning;
-//   * the four warps read their 32 TMEM lanes with tcgen05.ld and write FP64.
+// Kernel structure (one CTA = one 128 x BN output tile, 6 warps):
+//   * the split kernel writes every slice pre-tiled: one contiguous chunk per
+//     (row tile, 32-wide K block) already in the no-swizzle K-major
+//     core-matrix order (8 rows x 16 bytes per core matrix) that the MMA
+//     descriptors read, so each stage is 2S plain bulk copies;
+//   * warp 4 (producer) streams the chunks with cp.async.bulk into a ring of
+//     2-4 stages, each guarded by a full/empty mbarrier pair;
+//   * warp 5 issues tcgen05.mma (cta_group::1, kind::f16, bf16 inputs, FP32
+//     accumulation in TMEM) and tcgen05.commit, which frees a stage when its
+//     MMAs have read it;
+//   * warps 0-3 wait for the last commit, read their 32 TMEM lanes with
+//     tcgen05.ld and write FP64;
+//   * every mbarrier wait is bounded; on timeout an error word is set and
+//     the kernel drains (bounded) and frees its TMEM before returning.
 #include <cuda_bf16.h>
 #include <string.h>
 
@@ -47,7 +52,6 @@ namespace {
 
 constexpr int TC_BM = 128;
 constexpr int TC_BK = 32;
-constexpr int TC_THREADS = 128;
 constexpr int kMaxTcProbs = 4;
 constexpr int kMaxSplitJobs = 2 * kMaxTcProbs * 2;  // probs x operands x terms
 constexpr long long kSpinLimit = 1ll << 22;         // bounded mbarrier waits (~1 s)
@@ -63,10 +67,11 @@ struct SplitSrc {
 
 struct SplitJob {
     SplitSrc src;
-    __nv_bfloat16* out;   // [S][Rpad][Kpad] per instance
+    __nv_bfloat16* out;   // per instance: [S][Rpad/RT][Kpad/32] chunks of RT x 32 (core-matrix order)
     int32_t* exps;        // [Rpad] per instance (biased FP64 exponent of the row max)
     int64_t out_stride, exp_stride;
     int32_t R, Rpad, Kpad;
+    int32_t RT;           // rows per chunk: 128 for A, the tile width for B
     int32_t batch;
     int32_t tiles_r, tiles_k, tile_begin;
 };
@@ -174,12 +179,18 @@ __global__ void __launch_bounds__(256) k_split_slices(const __grid_constant__ Sp
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     __nv_bfloat16* out = J.out + (int64_t)inst * J.out_stride;
     const int64_t slice = (int64_t)J.Rpad * J.Kpad;
+    const int nkb = J.Kpad / 32, RT = J.RT;
+    const int kb = (J.src.koff + k0) / 32;  // k within the block = tx
     for (int rr = ty; rr < 32; rr += 8) {
         const int r = r0 + rr;
         if (r >= J.Rpad) continue;
         int d[S];
         digits<S>(t[rr][tx], ex[rr], d);
-        const int64_t o = (int64_t)r * J.Kpad + J.src.koff + k0 + tx;
+        // chunk (r / RT, kb) of RT x 32 elements in core-matrix order:
+        // [k/8][row/8][row%8][k%8]
+        const int rt = r / RT, ri = r % RT;
+        const int64_t o = ((int64_t)rt * nkb + kb) * (RT * 32) + ((tx >> 3) * (RT >> 3) + (ri >> 3)) * 64 +
+                          (ri & 7) * 8 + (tx & 7);
 #pragma unroll
         for (int p = 0; p < S; ++p) {
             const float w = ldexpf((float)d[p], -7 * p);
@@ -258,9 +269,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
 
 __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                        uint32_t accum) {
@@ -311,22 +319,44 @@ __device__ __forceinline__ double scale_pow2(double r, int e) {
     return ldexp(r, e);
 }
 
+__device__ __forceinline__ void mbar_expect_tx(uint32_t addr, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(addr), "r"(bytes) : "memory");
+}
+
+// 1-D bulk copy global -> shared, completing `bytes` on the mbarrier.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(mbar)
+        : "memory");
+}
+
 template <int S, int BN>
 struct TcSmem {
     static constexpr int kA = S * TC_BM * TC_BK * 2;   // bytes of A slices per stage
     static constexpr int kB = S * BN * TC_BK * 2;      // bytes of B slices per stage
     static constexpr int kStage = kA + kB;
-    static constexpr int kBytes = 2 * kStage + 1024 + 64;
+    static constexpr int kBudget = 225 * 1024;
+    static constexpr int kStages = (kBudget / kStage) > 4 ? 4 : (kBudget / kStage);
+    static constexpr int kBytes = kStages * kStage + 1024 + 256;
+    static_assert(kStages >= 2, "at least two pipeline stages");
 };
 
+// Warp roles (192 threads): warps 0-3 epilogue (TMEM lanes 0-127), warp 4
+// producer (bulk copies into a kStages ring), warp 5 MMA issuer.
+constexpr int TC_THREADS2 = 192;
+
 template <int S, int BN>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_gemm_tc(const __grid_constant__ TcLaunch L) {
+__global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constant__ TcLaunch L) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // 1024-byte aligned carve
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     using SM = TcSmem<S, BN>;
-    uint64_t* bars = (uint64_t*)(smem + 2 * SM::kStage);  // bars[0], bars[1]
-    uint32_t* tmem_slot = (uint32_t*)(bars + 2);
+    constexpr int NS = SM::kStages;
+    uint64_t* full = (uint64_t*)(smem + NS * SM::kStage);
+    uint64_t* empty = full + NS;
+    uint64_t* done = empty + NS;
+    uint32_t* tmem_slot = (uint32_t*)(done + 1);
+    int* flags = (int*)(tmem_slot + 1);  // [0] error seen
 
     const int tile = blockIdx.x;
     int pi = 0;
@@ -338,12 +368,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_gemm_tc(const __grid_constant
     const int per = P.tiles_m * P.tiles_n;
     const int inst = local / per;
     local -= inst * per;
-    const int m0 = (local / P.tiles_n) * TC_BM;
-    const int n0 = (local % P.tiles_n) * BN;
+    const int mt = local / P.tiles_n, ntile = local % P.tiles_n;
+    const int m0 = mt * TC_BM, n0 = ntile * BN;
     if (P.lower_only && n0 >= m0 + TC_BM) return;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr int NACC = S < 6 ? S : 6;  // TMEM accumulators (levels 0..NACC-1, last one lumps the rest)
+    constexpr int NACC = S < 6 ? S : 6;
     constexpr int kUsed = NACC * BN;
     constexpr int kCols = kUsed <= 32 ? 32 : kUsed <= 64 ? 64 : kUsed <= 128 ? 128 : kUsed <= 256 ? 256 : 512;
     static_assert(kUsed <= 512, "TMEM columns");
@@ -354,89 +384,93 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_gemm_tc(const __grid_constant
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (tid == 0) {
-        mbar_init(smem_u32(&bars[0]), 1);
-        mbar_init(smem_u32(&bars[1]), 1);
+    if (tid == 32) {
+        for (int i = 0; i < NS; ++i) {
+            mbar_init(smem_u32(&full[i]), 1);
+            mbar_init(smem_u32(&empty[i]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        flags[0] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    const __nv_bfloat16* Ag = P.A + (int64_t)inst * P.strideA;
-    const __nv_bfloat16* Bg = P.B + (int64_t)inst * P.strideB;
-    const int64_t sliceA = (int64_t)P.Mpad * P.Kpad;
-    const int64_t sliceB = (int64_t)P.Npad * P.Kpad;
     const int nkb = P.Kpad / TC_BK;
-    constexpr uint32_t idesc = make_idesc(TC_BM, BN);
     const uint32_t sbase = smem_u32(smem);
-    bool ok = true;
-    uint32_t inited = 0;  // bit l: accumulator l written (thread 0 only)
+    // chunk bases: A chunk (p, mt, kb) and B chunk (q, ntile, kb)
+    const unsigned char* Ag = (const unsigned char*)(P.A + (int64_t)inst * P.strideA);
+    const unsigned char* Bg = (const unsigned char*)(P.B + (int64_t)inst * P.strideB);
+    const int64_t a_slice = (int64_t)P.Mpad * P.Kpad * 2, b_slice = (int64_t)P.Npad * P.Kpad * 2;
+    const int64_t a_tile = (int64_t)mt * nkb * (TC_BM * TC_BK * 2), b_tile = (int64_t)ntile * nkb * (BN * TC_BK * 2);
 
-    for (int kb = 0; kb < nkb; ++kb) {
-        const int st = kb & 1;
-        if (kb >= 2) {
-            if (!mbar_wait(smem_u32(&bars[st]), (uint32_t)(((kb - 2) >> 1) & 1))) ok = false;
-        }
-        if (__syncthreads_or(!ok)) break;
-        const uint32_t sA = sbase + st * SM::kStage;
-        const uint32_t sB = sA + SM::kA;
-        const int k0 = kb * TC_BK;
-        // A: S slices x 128 rows x 4 chunks of 8 elements
-        constexpr int nA = S * TC_BM * 4;
-        constexpr int nB = S * BN * 4;
-        for (int c = tid; c < nA + nB; c += TC_THREADS) {
-            if (c < nA) {
-                const int p = c / (TC_BM * 4);
-                const int rem = c - p * TC_BM * 4;
-                const int r = rem >> 2, kc = rem & 3;
-                const __nv_bfloat16* src = Ag + p * sliceA + (int64_t)(m0 + r) * P.Kpad + k0 + kc * 8;
-                const uint32_t dst = sA + p * (TC_BM * TC_BK * 2) + (kc * (TC_BM / 8) + (r >> 3)) * 128 + (r & 7) * 16;
-                cp_async16(dst, src);
-            } else {
-                const int cc = c - nA;
-                const int q = cc / (BN * 4);
-                const int rem = cc - q * BN * 4;
-                const int r = rem >> 2, kc = rem & 3;
-                const __nv_bfloat16* src = Bg + q * sliceB + (int64_t)(n0 + r) * P.Kpad + k0 + kc * 8;
-                const uint32_t dst = sB + q * (BN * TC_BK * 2) + (kc * (BN / 8) + (r >> 3)) * 128 + (r & 7) * 16;
-                cp_async16(dst, src);
-            }
-        }
-        asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-            for (int s = 0; s < TC_BK / 16; ++s) {
-#pragma unroll
+    if (warp == 4) {
+        // producer
+        if (lane == 0) {
+            for (int kb = 0; kb < nkb; ++kb) {
+                const int st = kb % NS, round = kb / NS;
+                if (kb >= NS && !mbar_wait(smem_u32(&empty[st]), (uint32_t)((round - 1) & 1))) {
+                    atomicExch(&flags[0], 1);
+                    break;
+                }
+                const uint32_t fb = smem_u32(&full[st]);
+                mbar_expect_tx(fb, (uint32_t)SM::kStage);
+                const uint32_t sA = sbase + st * SM::kStage, sB = sA + SM::kA;
+#pragma unroll 1
                 for (int p = 0; p < S; ++p) {
-                    const uint64_t ad = make_desc(sA + p * (TC_BM * TC_BK * 2) + s * 2 * (TC_BM / 8) * 128,
-                                                  (TC_BM / 8) * 128, 128);
-#pragma unroll
-                    for (int q = 0; q + p < S; ++q) {
-                        const int l = (p + q) < NACC ? (p + q) : NACC - 1;
-                        const uint64_t bd = make_desc(sB + q * (BN * TC_BK * 2) + s * 2 * (BN / 8) * 128,
-                                                      (BN / 8) * 128, 128);
-                        tc_mma(tmem + l * BN, ad, bd, idesc, (inited >> l) & 1u);
-                        inited |= 1u << l;
-                    }
+                    bulk_g2s(sA + p * (TC_BM * TC_BK * 2), Ag + p * a_slice + a_tile + (int64_t)kb * (TC_BM * TC_BK * 2),
+                             TC_BM * TC_BK * 2, fb);
+                    bulk_g2s(sB + p * (BN * TC_BK * 2), Bg + p * b_slice + b_tile + (int64_t)kb * (BN * TC_BK * 2),
+                             BN * TC_BK * 2, fb);
                 }
             }
-            tc_commit(smem_u32(&bars[st]));
+        }
+    } else if (warp == 5) {
+        // MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = make_idesc(TC_BM, BN);
+            uint32_t inited = 0;
+            for (int kb = 0; kb < nkb; ++kb) {
+                const int st = kb % NS, round = kb / NS;
+                if (!mbar_wait(smem_u32(&full[st]), (uint32_t)(round & 1)) || flags[0]) {
+                    atomicExch(&flags[0], 1);
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t sA = sbase + st * SM::kStage, sB = sA + SM::kA;
+#pragma unroll
+                for (int ks = 0; ks < TC_BK / 16; ++ks) {
+#pragma unroll
+                    for (int p = 0; p < S; ++p) {
+                        const uint64_t ad = make_desc(sA + p * (TC_BM * TC_BK * 2) + ks * 2 * (TC_BM / 8) * 128,
+                                                      (TC_BM / 8) * 128, 128);
+#pragma unroll
+                        for (int q = 0; q + p < S; ++q) {
+                            const int l = (p + q) < NACC ? (p + q) : NACC - 1;
+                            const uint64_t bd = make_desc(sB + q * (BN * TC_BK * 2) + ks * 2 * (BN / 8) * 128,
+                                                          (BN / 8) * 128, 128);
+                            tc_mma(tmem + l * BN, ad, bd, idesc, (inited >> l) & 1u);
+                            inited |= 1u << l;
+                        }
+                    }
+                }
+                tc_commit(smem_u32(&empty[st]));  // frees the stage when these MMAs finish
+            }
+            tc_commit(smem_u32(done));  // all issued MMAs
         }
     }
 
-    // wait for the last commit (covers every MMA issued before it)
-    if (ok && nkb > 0) {
-        const int kl = nkb - 1;
-        if (!mbar_wait(smem_u32(&bars[kl & 1]), (uint32_t)((kl >> 1) & 1))) ok = false;
+    // epilogue warps 0-3
+    bool ok = true;
+    if (warp < 4) {
+        if (!mbar_wait(smem_u32(done), 0)) ok = false;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const bool all_ok = !__syncthreads_or(!ok);
+    const bool all_ok = !__syncthreads_or(!ok || flags[0] != 0);
 
-    if (all_ok) {
+    if (all_ok && warp < 4) {
         const int m = m0 + warp * 32 + lane;
         const int64_t mrow = m;
         const int eAm = (m < P.M) ? P.eA[(int64_t)inst * P.strideEA + m] : 0;
@@ -466,7 +500,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_gemm_tc(const __grid_constant
                     double r = 0.0;
                     const int eBn = eB[n];
                     if (eAm != 0 && eBn != 0) {
-                        // exact FP32-pair sum of the level accumulators
                         float hi = v[0][i], lo = 0.f;
 #pragma unroll
                         for (int l = 1; l < NACC; ++l) {
@@ -491,19 +524,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_gemm_tc(const __grid_constant
                 }
             }
         }
-    } else if (tid == 0 && L.err != nullptr) {
+    } else if (!all_ok && tid == 0 && L.err != nullptr) {
         atomicExch(L.err, SGB_ERR_TIMEOUT);
     }
-
-    if (!all_ok) {
-        // drain: MMAs may still be in flight; wait (bounded) on both stages
-        // before the TMEM is released.
-        if (tid == 0) {
-            for (int st = 0; st < 2; ++st) {
-                const uint32_t a = smem_u32(&bars[st]);
-                mbar_wait(a, 0);
-                mbar_wait(a, 1);
-            }
+    if (!all_ok && tid == 0) {
+        // drain (bounded): the final commit, then any stage still being filled
+        mbar_wait(smem_u32(done), 0);
+        for (int i = 0; i < NS; ++i) {
+            mbar_wait(smem_u32(&full[i]), 0);
+            mbar_wait(smem_u32(&full[i]), 1);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -522,7 +551,7 @@ cudaError_t set_smem_attr() {
 
 template <int S, int BN>
 cudaError_t launch_tc(TcLaunch& L, int total_tiles, cudaStream_t s) {
-    k_gemm_tc<S, BN><<<total_tiles, TC_THREADS, TcSmem<S, BN>::kBytes, s>>>(L);
+    k_gemm_tc<S, BN><<<total_tiles, TC_THREADS2, TcSmem<S, BN>::kBytes, s>>>(L);
     return cudaGetLastError();
 }
 
@@ -627,6 +656,7 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
             ja.exp_stride = inst_stride_bytes / 4;
             ja.R = p.M;
             ja.Rpad = (int32_t)Mpad;
+            ja.RT = TC_BM;
             ja.Kpad = (int32_t)Kalloc;
             ja.batch = p.batch;
             ja.tiles_r = (int32_t)ceil_div(Mpad, 32);
@@ -641,6 +671,7 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
             jb.exps = eB;
             jb.R = p.N;
             jb.Rpad = (int32_t)Npad;
+            jb.RT = bn;
             jb.tiles_r = (int32_t)ceil_div(Npad, 32);
             for (SplitJob* j : {&ja, &jb}) {
                 if (SL.nj >= kMaxSplitJobs) return cudaErrorInvalidValue;

@@ -102,6 +102,15 @@ cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, R
 template <typename T>
 using GemmFn = cudaError_t (*)(void* ctx, GemmProb<T>* probs, int np, cudaStream_t s);
 
+// The same column-block factorization as one cooperative persistent launch
+// (sgb_panel.cu).  `bar` is two unsigned words of scratch; `status` receives
+// SGB_ERR_TIMEOUT if a grid barrier gives up.  Not for use under stream
+// capture (cooperative launch).
+template <typename T>
+cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, RowSet<T> r2, T* tinv,
+                                    unsigned* bar, int32_t* status, int32_t* info, int64_t info_row0,
+                                    cudaStream_t s);
+
 // Full triangular inverse of `batch` lower-triangular m x m blocks:
 // Linv_j = L_j^{-1} (zeros above the diagonal).  Scratch: batch*kTile*m T.
 // The row-sweep products go through `fn(fnctx, ...)` when given, else the
