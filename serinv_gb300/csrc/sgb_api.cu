@@ -109,27 +109,41 @@ cudaError_t ctx_gemm(void* c, GemmProb<T>* pr, int np, cudaStream_t s) {
     return run_gemm<T>(*(const Ctx*)c, pr, np, s);
 }
 
-// Tensor-core scratch of one row-sweep product of a batched triangular
-// inversion of `batch` m x m blocks (32-row strips: M = 32, N, K <= m).
+// Tensor-core scratch of the largest grouped product of a batched
+// recursive-doubling inversion of `batch` m x m blocks: at level h, up to
+// four pair problems of h x h (K = h) per launch.
 size_t trtri_tc_bytes(int S, int64_t m, int64_t batch) {
-    const int64_t Npad = ceil_div(m, kTcBN) * kTcBN, Kpad = ceil_div(m, 32) * 32;
-    const size_t per = (size_t)S * (128 + Npad) * Kpad * 2 + (size_t)(128 + Npad) * 4;
-    return (size_t)batch * ((per + 255) / 256 * 256) + 512;
+    size_t best = 0;
+    for (int64_t h = kTile; h < m; h *= 2) {
+        const int64_t pairs = (m / h + 1) / 2;
+        const int64_t group = pairs < 4 ? pairs : 4;
+        const int64_t Mpad = ceil_div(h, 128) * 128, Npad = ceil_div(h, kTcBN) * kTcBN, Kpad = ceil_div(h, 32) * 32;
+        const size_t per = (size_t)S * (Mpad + Npad) * Kpad * 2 + (size_t)(Mpad + Npad) * 4;
+        const size_t bytes = (size_t)group * ((size_t)batch * ((per + 255) / 256 * 256) + 256);
+        best = bytes > best ? bytes : best;
+    }
+    return best + 512;
 }
 
-// Matrices per chunk of a tensor-core batched inversion (bounds the scratch).
+// Blocks per chunk of a batched inversion (bounds the scratch).
 constexpr int64_t kTrtriChunk = 64;
 
-// Batched L^{-1}: SIMT products natively, tensor-core products in mixed
-// mode (in chunks of kTrtriChunk blocks so the slice scratch stays bounded).
+int64_t trtri_chunk(int64_t batch) { return batch < kTrtriChunk ? batch : kTrtriChunk; }
+
+// Scratch elements of trtri_run for `batch` m x m blocks.
+size_t trtri_scratch_elems(int64_t m, int64_t batch) { return (size_t)trtri_chunk(batch) * m * m; }
+
+// Batched L^{-1} in chunks of kTrtriChunk blocks: SIMT products natively,
+// tensor-core products in mixed mode.
 template <typename T>
 cudaError_t trtri_run(const Ctx& cx, const T* L, int64_t m, int64_t batch, T* Linv, T* scratch, cudaStream_t s) {
     const int64_t mm = m * m;
-    if (cx.slices == 0 || m <= kTile) return trtri_batched<T>(L, m, mm, m, batch, Linv, m, mm, scratch, s);
     for (int64_t j0 = 0; j0 < batch; j0 += kTrtriChunk) {
         const int64_t nb = (batch - j0) < kTrtriChunk ? (batch - j0) : kTrtriChunk;
-        cudaError_t e = trtri_batched<T>(L + j0 * mm, m, mm, m, nb, Linv + j0 * mm, m, mm, scratch, s,
-                                         ctx_gemm<T>, (void*)&cx);
+        cudaError_t e = cx.slices == 0
+                            ? trtri_batched<T>(L + j0 * mm, m, mm, m, nb, Linv + j0 * mm, m, mm, scratch, s)
+                            : trtri_batched<T>(L + j0 * mm, m, mm, m, nb, Linv + j0 * mm, m, mm, scratch, s,
+                                               ctx_gemm<T>, (void*)&cx);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -163,7 +177,7 @@ struct PobtafWs {
         tc = c.take(tc_bytes);
         // mixed precision only: L_ii^{-1} and its triangular-inverse scratch
         linv = c.take(S ? sizeof(T) * m->b * m->b : 0);
-        trtri = c.take(S ? sizeof(T) * kTile * m->b : 0);
+        trtri = c.take(S ? sizeof(T) * trtri_scratch_elems(m->b, 1) : 0);
         total = c.off;
     }
 };
@@ -187,7 +201,7 @@ struct PobtasiWs {
         tc = c.take(tc_bytes);
         linv = c.take(sizeof(T) * n * b * b);
         linv_tip = c.take(sizeof(T) * a * a);
-        trtri = c.take(sizeof(T) * n * kTile * mx);
+        trtri = c.take(sizeof(T) * (trtri_scratch_elems((int64_t)mx, (int64_t)n)));
         uv = c.take(sizeof(T) * (b + a) * b);
         xt = c.take(sizeof(T) * (b + a) * b);
         w = c.take(sizeof(T) * b * b);
@@ -204,7 +218,7 @@ struct PobtasWs {
         Carve c;
         linv = c.take(sizeof(T) * n * b * b);
         linv_tip = c.take(sizeof(T) * a * a);
-        trtri = c.take(sizeof(T) * n * kTile * mx);
+        trtri = c.take(sizeof(T) * trtri_scratch_elems((int64_t)mx, (int64_t)n));
         y = c.take(sizeof(T) * mx * (size_t)nrhs);
         total = c.off;
     }
@@ -543,8 +557,9 @@ int pobtas_native(const sgb_bta* m, T* Bm, int64_t nrhs, int64_t ldb, char trans
     auto Bi = [&](int64_t i) { return Bm + i * b * ldb; };
 
     if (nrhs == 0) return SGB_OK;
-    SGB_TRY(trtri_batched<T>(D, b, bb, b, n, Linv, b, bb, trs, s));
-    if (a && !partial) SGB_TRY(trtri_batched<T>(Tp, a, a * a, a, 1, Ltinv, a, a * a, trs, s));
+    Ctx native;
+    SGB_TRY(trtri_run<T>(native, D, b, n, Linv, trs, s));
+    if (a && !partial) SGB_TRY(trtri_run<T>(native, Tp, a, 1, Ltinv, trs, s));
 
     if (trans == 'N') {
         const int64_t last = partial ? n - 1 : n;

@@ -112,7 +112,7 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
                                     cudaStream_t s);
 
 // Full triangular inverse of `batch` lower-triangular m x m blocks:
-// Linv_j = L_j^{-1} (zeros above the diagonal).  Scratch: batch*kTile*m T.
+// Linv_j = L_j^{-1} (zeros above the diagonal).  Scratch: batch*m*m T.
 // The row-sweep products go through `fn(fnctx, ...)` when given, else the
 // SIMT kernel.
 template <typename T>

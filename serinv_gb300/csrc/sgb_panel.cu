@@ -10,10 +10,11 @@
 //   --- grid barrier ---
 //   B(p)  all CTAs: rows below the tile <- rows * tile^{-T} (8-row chunks);
 //   --- grid barrier ---
-//   C(p)  CTA 0 updates only the next diagonal tile (p+1, p+1) and moves on
-//         to A(p+1) at once (lookahead); CTAs 1.. apply the rank-32 update
-//         to the rest of the trailing panel.  The barrier after A(p+1) also
-//         closes C(p), which B(p+1) needs.
+//   C(p)  CTAs 1-4 first update the next diagonal tile (p+1, p+1), eight
+//         rows each, and count themselves on a flag; CTA 0 waits for the
+//         flag and factors that tile at once (lookahead) while CTAs 1..
+//         apply the rank-32 update to the rest of the trailing panel.  The
+//         barrier after A(p+1) also closes C(p), which B(p+1) needs.
 //
 // Grid barriers are a counter + generation pair in global memory with a
 // bounded spin: a barrier that does not complete within the limit sets the
@@ -24,6 +25,7 @@
 #include <math.h>
 
 #include "sgb_internal.cuh"
+#include "sgb_tile.cuh"
 
 namespace sgb {
 
@@ -43,7 +45,7 @@ struct PanelArgs {
     T* tinv;  // 32 x 32 global scratch
     int32_t* info;
     int64_t row0;
-    unsigned* bar;    // [0] arrivals, [1] generation; zero at launch
+    unsigned* bar;    // [0] arrivals, [1] generation, [2] diagonal-tile pieces; zero at launch
     int32_t* status;  // SGB_ERR_TIMEOUT on a stuck barrier
 };
 
@@ -51,13 +53,6 @@ template <typename T>
 __device__ __forceinline__ T ldcg(const T* p) {
     return __ldcg(p);
 }
-
-template <typename T>
-__device__ __forceinline__ T rsq(T x);
-template <>
-__device__ __forceinline__ double rsq<double>(double x) { return rsqrt(x); }
-template <>
-__device__ __forceinline__ float rsq<float>(float x) { return rsqrtf(x); }
 
 // Grid barrier; returns false (on every thread of the CTA) if it timed out.
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, unsigned& epoch, int32_t* status,
@@ -90,102 +85,6 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, un
     return *sflag != 0;
 }
 
-template <typename T>
-struct Smem {
-    T s[kTile][kTile + 1];
-    T x[kTile][kTile + 1];
-    T tmp[kTile][kTile + 1];
-    T yv[kTile];
-    int fail;
-    int flag;
-};
-
-// Recursive-doubling inverse of the (identity padded) lower tile s into x.
-template <typename T>
-__device__ void tile_inverse_dev(Smem<T>& S) {
-    const int tid = threadIdx.x;
-    for (int e = tid; e < kTile * kTile; e += NT) S.x[e / kTile][e % kTile] = T(0);
-    __syncthreads();
-    if (tid < 32) {
-        const int blk = tid >> 3, jj = tid & 7, b0 = blk * 8, j = b0 + jj;
-        for (int r = j; r < b0 + 8; ++r) {
-            T sum = (r == j) ? T(1) : T(0);
-            for (int k = j; k < r; ++k) sum = fma(-S.s[r][k], S.x[k][j], sum);
-            S.x[r][j] = sum * S.yv[r];
-        }
-    }
-    __syncthreads();
-    for (int h = 8; h < kTile; h *= 2) {
-        const int nblk = kTile / (2 * h);
-        for (int e = tid; e < nblk * h * h; e += NT) {
-            const int bi = e / (h * h), rem = e % (h * h), r = rem / h, c = rem % h, o = bi * 2 * h;
-            T sum = T(0);
-            for (int k = c; k < h; ++k) sum = fma(S.s[o + h + r][o + k], S.x[o + k][o + c], sum);
-            S.tmp[o + h + r][o + c] = sum;
-        }
-        __syncthreads();
-        for (int e = tid; e < nblk * h * h; e += NT) {
-            const int bi = e / (h * h), rem = e % (h * h), r = rem / h, c = rem % h, o = bi * 2 * h;
-            T sum = T(0);
-            for (int k = 0; k <= r; ++k) sum = fma(S.x[o + h + r][o + h + k], S.tmp[o + h + k][o + c], sum);
-            S.x[o + h + r][o + c] = -sum;
-        }
-        __syncthreads();
-    }
-}
-
-// A(p): Cholesky + inverse of the diagonal tile at `tile` (nb <= 32), by one CTA.
-template <typename T>
-__device__ void factor_tile(Smem<T>& S, T* tile, int64_t ld, int nb, int zero_right, T* tinv, int32_t* info,
-                            int64_t row0) {
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int e = tid; e < kTile * kTile; e += NT) {
-        const int r = e / kTile, c = e % kTile;
-        T v = T(0);
-        if (r < nb && c <= r) v = ldcg(tile + (int64_t)r * ld + c);
-        else if (r >= nb && r == c) v = T(1);
-        S.s[r][c] = v;
-    }
-    if (tid == 0) S.fail = 0;
-    if (tid < kTile) S.yv[tid] = T(1);
-    __syncthreads();
-    const int wk = warp == 0 || warp == 4 ? -1 : (warp < 4 ? warp - 1 : warp - 2);
-    for (int j = 0; j < nb; ++j) {
-        if (warp == 0) {
-            const T d = S.s[j][j];
-            const bool bad = !(d > T(0)) || !isfinite((double)d);
-            const T y = bad ? T(NAN) : rsq<T>(d);
-            if (lane > j && lane < nb) S.s[lane][j] *= y;
-            if (lane == j) {
-                S.s[j][j] = d * y;
-                S.yv[j] = y;
-                if (bad && S.fail == 0) S.fail = j + 1;
-            }
-        } else if (wk >= 0 && j >= 1) {
-            const int c0 = j + 1, k = j - 1, w = nb - c0;
-            for (int e = wk * 32 + lane; e < w * w; e += 6 * 32) {
-                const int rr = c0 + e / w, cc = c0 + e % w;
-                if (cc <= rr) S.s[rr][cc] = fma(-S.s[rr][k], S.s[cc][k], S.s[rr][cc]);
-            }
-        }
-        __syncthreads();
-        if (warp == 0 && j + 1 < nb && lane >= j + 1 && lane < nb)
-            S.s[lane][j + 1] = fma(-S.s[lane][j], S.s[j + 1][j], S.s[lane][j + 1]);
-    }
-    __syncthreads();
-    if (tid == 0 && S.fail != 0 && info != nullptr) atomicCAS(info, 0, (int32_t)(row0 + S.fail));
-    tile_inverse_dev<T>(S);
-    for (int e = tid; e < nb * nb; e += NT) {
-        const int r = e / nb, c = e % nb;
-        tile[(int64_t)r * ld + c] = (c <= r) ? S.s[r][c] : T(0);
-        tinv[r * kTile + c] = S.x[r][c];
-    }
-    for (int e = tid; e < nb * zero_right; e += NT) {
-        const int r = e / zero_right, c = e % zero_right;
-        tile[(int64_t)r * ld + nb + c] = T(0);
-    }
-}
-
 // Row r of the unified row space [D rows c1..m) ++ r1 rows ++ r2 rows.
 template <typename T>
 __device__ __forceinline__ T* row_ptr(const PanelArgs<T>& a, int64_t c1, int64_t r) {
@@ -197,7 +96,7 @@ __device__ __forceinline__ T* row_ptr(const PanelArgs<T>& a, int64_t c1, int64_t
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT) k_factor_panel(const __grid_constant__ PanelArgs<T> a) {
+__global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ PanelArgs<T> a) {
     __shared__ Smem<T> S;
     const int tid = threadIdx.x;
     const unsigned G = gridDim.x;
@@ -226,9 +125,18 @@ __global__ void __launch_bounds__(NT) k_factor_panel(const __grid_constant__ Pan
             T* rp = r < nrows ? row_ptr(a, c1, r) + c0 : nullptr;
             S.tmp[ty][tx] = (rp != nullptr && tx < w) ? ldcg(rp + tx) : T(0);
             __syncthreads();
-            T acc = T(0);
-            for (int k = 0; k <= tx && k < w; ++k) acc = fma(S.tmp[ty][k], S.x[tx][k], acc);
-            if (rp != nullptr && tx < w) rp[tx] = acc;
+            // (strip * tinv^T)[ty][tx] = sum_{k <= tx} strip[ty][k] tinv[tx][k], four accumulators
+            const int kend = (tx < w - 1 ? tx : w - 1) + 1;
+            T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+            int k = 0;
+            for (; k + 3 < kend; k += 4) {
+                a0 = fma(S.tmp[ty][k], S.x[tx][k], a0);
+                a1 = fma(S.tmp[ty][k + 1], S.x[tx][k + 1], a1);
+                a2 = fma(S.tmp[ty][k + 2], S.x[tx][k + 2], a2);
+                a3 = fma(S.tmp[ty][k + 3], S.x[tx][k + 3], a3);
+            }
+            for (; k < kend; ++k) a0 = fma(S.tmp[ty][k], S.x[tx][k], a0);
+            if (rp != nullptr && tx < w) rp[tx] = (a0 + a1) + (a2 + a3);
             __syncthreads();
         }
         if (!grid_barrier(a.bar, G, epoch, a.status, &S.flag)) return;
@@ -300,13 +208,51 @@ __global__ void __launch_bounds__(NT) k_factor_panel(const __grid_constant__ Pan
                 }
             __syncthreads();
         };
+        // The next diagonal tile (p+1, p+1) is on the critical path: CTAs
+        // 1-4 update 8 of its rows each (lower part) and publish them on a
+        // counter; CTA 0 waits for the four pieces and factors the tile
+        // while the other CTAs run the rest of the trailing update.
         if (blockIdx.x == 0) {
-            do_tile(0);  // the next diagonal tile, then its factorization right away
-            const int64_t c2 = c1;
-            const int w2 = (int)((m - c2) < kTile ? (m - c2) : kTile);
-            factor_tile<T>(S, a.diag + c2 * a.ldd + c2, a.ldd, w2, (int)(m - c2 - w2), a.tinv, a.info,
-                           a.row0 + c2);
+            if (tid == 0) {
+                const unsigned target = 4u * (unsigned)(p + 1);
+                long long spins = 0;
+                int ok = 1;
+                while (atomicAdd(&a.bar[2], 0u) < target) {
+                    if (++spins > kBarrierSpin) {
+                        ok = 0;
+                        atomicExch(a.status, SGB_ERR_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+                __threadfence();
+                S.flag = ok;
+            }
+            __syncthreads();
+            if (!S.flag) return;
+            const int w2 = (int)((m - c1) < kTile ? (m - c1) : kTile);
+            factor_tile<T>(S, a.diag + c1 * a.ldd + c1, a.ldd, w2, (int)(m - c1 - w2), a.tinv, a.info,
+                           a.row0 + c1);
         } else {
+            if (blockIdx.x <= 4) {
+                const int piece = (int)blockIdx.x - 1;
+                const int64_t rows_d = (m - c1) < kTile ? (m - c1) : kTile;
+                for (int e = tid; e < kTile * kTile; e += NT) {
+                    const int r = e / kTile, k = e % kTile;
+                    S.tmp[r][k] = (r < rows_d && k < w) ? ldcg(Bpan + (int64_t)r * a.ldd + k) : T(0);
+                }
+                __syncthreads();
+                const int r = piece * 8 + ty, c = tx;
+                if (r < rows_d && c <= r) {
+                    T acc = T(0);
+                    for (int k = 0; k < w; ++k) acc = fma(S.tmp[r][k], S.tmp[c][k], acc);
+                    T* cp = a.diag + (c1 + r) * a.ldd + c1 + c;
+                    *cp = ldcg(cp) - acc;
+                }
+                __threadfence();
+                __syncthreads();
+                if (tid == 0) atomicAdd(&a.bar[2], 1u);
+            }
             for (int64_t t = 1 + (blockIdx.x - 1); t < total; t += (G > 1 ? G - 1 : 1)) do_tile(t);
         }
         if (!grid_barrier(a.bar, G, epoch, a.status, &S.flag)) return;
@@ -330,7 +276,7 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_factor_panel<double>, NT, 0);
         if (e != cudaSuccess) return e;
-        int per = occ < 2 ? occ : 2;
+        int per = occ < 1 ? occ : 1;  // one CTA per SM: cheaper barriers, full FP64 pipe per CTA
         if (per < 1) return cudaErrorLaunchOutOfResources;
         g_panel_grid[dev] = sms * per;
     }
@@ -350,7 +296,7 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
     a.row0 = info_row0;
     a.bar = bar;
     a.status = status;
-    e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s);
+    e = cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     void* args[] = {(void*)&a};
     prof_before(s);

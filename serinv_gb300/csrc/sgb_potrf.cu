@@ -8,159 +8,33 @@
 //   [D_i; Lo_i; Ar_i] — the diagonal block and the rows below it are
 //   factored together, tile column by tile column, so the TRSMs of
 //   src/serinv/algs/pobtaf.py:120-139 become part of the same sweep.
-// * trtri_batched: L^{-1} of many blocks at once (row sweep over tiles).
+// * trtri_batched: L^{-1} of many blocks at once (recursive doubling over
+//   32-row tiles: a handful of grouped, batched products per level).
 #include <math.h>
 #include <string.h>
 
 #include "sgb_internal.cuh"
+#include "sgb_tile.cuh"
 
 namespace sgb {
 
 namespace {
 
-constexpr int NT = 256;
+constexpr int NT = kTileThreads;
 
-template <typename T>
-__device__ __forceinline__ T sgb_rsqrt(T x);
-template <>
-__device__ __forceinline__ double sgb_rsqrt<double>(double x) { return rsqrt(x); }
-template <>
-__device__ __forceinline__ float sgb_rsqrt<float>(float x) { return rsqrtf(x); }
-
-// Inverse of the lower-triangular tile s (32 x 32, identity-padded beyond
-// nb) into x, given the reciprocal diagonal yv.  Recursive doubling keeps
-// every step a small parallel product, so no thread runs a long dependent
-// chain of FP64 operations (each FP64 warp instruction costs ~64 issue
-// cycles on this part):
-//   leaves: the four 8 x 8 diagonal blocks by forward substitution;
-//   level 1: X21 = -X22 (L21 X11) for the two 16 x 16 blocks;
-//   level 2: the same for the 32 x 32 tile.
-// Requires all NT threads; ends with a barrier.
-template <typename T>
-__device__ __forceinline__ void tile_inverse(T (*s)[kTile + 1], T (*x)[kTile + 1], T (*tmp)[kTile + 1],
-                                             const T* yv) {
-    const int tid = threadIdx.x;
-    for (int e = tid; e < kTile * kTile; e += NT) x[e / kTile][e % kTile] = T(0);
-    __syncthreads();
-    if (tid < 32) {  // leaves: 4 blocks x 8 columns
-        const int blk = tid >> 3, jj = tid & 7, b0 = blk * 8, j = b0 + jj;
-        for (int r = j; r < b0 + 8; ++r) {
-            T sum = (r == j) ? T(1) : T(0);
-            for (int k = j; k < r; ++k) sum = fma(-s[r][k], x[k][j], sum);
-            x[r][j] = sum * yv[r];
-        }
-    }
-    __syncthreads();
-#pragma unroll 1
-    for (int h = 8; h < kTile; h *= 2) {  // block size h -> 2h
-        const int nblk = kTile / (2 * h);
-        // tmp = L21 X11 for every 2h-block (h x h each)
-        for (int e = tid; e < nblk * h * h; e += NT) {
-            const int bi = e / (h * h), rem = e % (h * h), r = rem / h, c = rem % h;
-            const int o = bi * 2 * h;
-            T sum = T(0);
-            for (int k = c; k < h; ++k) sum = fma(s[o + h + r][o + k], x[o + k][o + c], sum);
-            tmp[o + h + r][o + c] = sum;
-        }
-        __syncthreads();
-        // X21 = -X22 tmp
-        for (int e = tid; e < nblk * h * h; e += NT) {
-            const int bi = e / (h * h), rem = e % (h * h), r = rem / h, c = rem % h;
-            const int o = bi * 2 * h;
-            T sum = T(0);
-            for (int k = 0; k <= r; ++k) sum = fma(x[o + h + r][o + h + k], tmp[o + h + k][o + c], sum);
-            x[o + h + r][o + c] = -sum;
-        }
-        __syncthreads();
-    }
-}
-
-// Cholesky of one <= 32 x 32 diagonal tile plus its inverse, with a
-// one-column lookahead.  Warp 0 (alone on its SM quarter, so nothing else
-// competes for that quarter's FP64 unit) owns the pivot chain: per column j
-// it forms 1/sqrt(d_j), scales column j, and after the barrier applies
-// column j to column j+1 only, so the next pivot is ready.  Warps on the
-// other three quarters (1-3, 5-7) meanwhile apply column j-1 to columns
-// j+1.. of the trailing triangle.  One barrier per column; the dependent
-// FP64 chain per column is rsqrt + one multiply + one FMA.
+// Diagonal tile: Cholesky + inverse (sgb_tile.cuh), pivot reported to info.
 template <typename T>
 __global__ void __launch_bounds__(NT)
 k_potrf_tile(T* A, int64_t ld, int nb, int zero_right, T* tinv, int32_t* info, int64_t row0) {
-    __shared__ T s[kTile][kTile + 1];
-    __shared__ T x[kTile][kTile + 1];
-    __shared__ T tmp[kTile][kTile + 1];
-    __shared__ T yv[kTile];
-    __shared__ int fail;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-
-    for (int e = tid; e < kTile * kTile; e += NT) {
-        const int r = e / kTile, c = e % kTile;
-        T v = T(0);
-        if (r < nb && c <= r) v = A[(int64_t)r * ld + c];
-        else if (r >= nb && r == c) v = T(1);  // identity padding
-        s[r][c] = v;
-    }
-    if (tid == 0) fail = 0;
-    if (tid < kTile) yv[tid] = T(1);
-    __syncthreads();
-
-    // update workers: warps 1,2,3,5,6,7 -> worker index 0..5
-    const int wk = warp == 0 || warp == 4 ? -1 : (warp < 4 ? warp - 1 : warp - 2);
-    const int nworkers = 6 * 32;
-    for (int j = 0; j < nb; ++j) {
-        if (warp == 0) {
-            const T d = s[j][j];
-            const bool bad = !(d > T(0)) || !isfinite((double)d);
-            const T y = bad ? T(NAN) : sgb_rsqrt<T>(d);
-            const int r = lane;
-            if (r > j && r < nb) s[r][j] *= y;
-            if (r == j) {
-                s[j][j] = d * y;
-                yv[j] = y;
-                if (bad && fail == 0) fail = j + 1;
-            }
-        } else if (wk >= 0 && j >= 1) {
-            // column j-1 applied to columns j+1 .. nb-1 (column j was done by warp 0)
-            const int c0 = j + 1, k = j - 1;
-            const int w = nb - c0;  // trailing width
-            for (int e = wk * 32 + lane; e < w * w; e += nworkers) {
-                const int rr = c0 + e / w, cc = c0 + e % w;
-                if (cc <= rr) s[rr][cc] = fma(-s[rr][k], s[cc][k], s[rr][cc]);
-            }
-        }
-        __syncthreads();
-        if (warp == 0 && j + 1 < nb) {  // lookahead: column j applied to column j+1
-            const int r = lane;
-            if (r >= j + 1 && r < nb) s[r][j + 1] = fma(-s[r][j], s[j + 1][j], s[r][j + 1]);
-        }
-    }
-    __syncthreads();
-
-    if (tid == 0 && fail != 0 && info != nullptr) atomicCAS(info, 0, (int32_t)(row0 + fail));
-
-    tile_inverse<T>(s, x, tmp, yv);
-
-    for (int e = tid; e < nb * nb; e += NT) {
-        const int r = e / nb, c = e - (e / nb) * nb;
-        A[(int64_t)r * ld + c] = (c <= r) ? s[r][c] : T(0);
-        tinv[r * kTile + c] = x[r][c];
-    }
-    // The reference's cholesky returns a zero strict upper triangle: clear
-    // the part of these rows to the right of the tile.
-    for (int e = tid; e < nb * zero_right; e += NT) {
-        const int r = e / zero_right, c = e - (e / zero_right) * zero_right;
-        A[(int64_t)r * ld + nb + c] = T(0);
-    }
+    __shared__ Smem<T> S;
+    factor_tile<T>(S, A, ld, nb, zero_right, tinv, info, row0);
 }
 
 // grid (tiles, batch): inverse of diagonal tile t of block blockIdx.y.
 template <typename T>
 __global__ void __launch_bounds__(NT)
 k_trtri_tiles(const T* L, int64_t ldl, int64_t strideL, int m, T* X, int64_t ldx, int64_t strideX) {
-    __shared__ T s[kTile][kTile + 1];
-    __shared__ T x[kTile][kTile + 1];
-    __shared__ T tmp[kTile][kTile + 1];
-    __shared__ T yv[kTile];
+    __shared__ Smem<T> S;
     const int t0 = blockIdx.x * kTile;
     const int nb = min(kTile, m - t0);
     const T* Lb = L + (int64_t)blockIdx.y * strideL + (int64_t)t0 * ldl + t0;
@@ -170,15 +44,15 @@ k_trtri_tiles(const T* L, int64_t ldl, int64_t strideL, int m, T* X, int64_t ldx
         T v = T(0);
         if (r < nb && c <= r) v = Lb[(int64_t)r * ldl + c];
         else if (r >= nb && r == c) v = T(1);
-        s[r][c] = v;
+        S.s[r][c] = v;
     }
     __syncthreads();
-    if (threadIdx.x < kTile) yv[threadIdx.x] = T(1) / s[threadIdx.x][threadIdx.x];
+    if (threadIdx.x < kTile) S.yv[threadIdx.x] = T(1) / S.s[threadIdx.x][threadIdx.x];
     __syncthreads();
-    tile_inverse<T>(s, x, tmp, yv);
+    tile_inverse_dev<T>(S);
     for (int e = threadIdx.x; e < nb * nb; e += NT) {
         const int r = e / nb, c = e - (e / nb) * nb;
-        Xb[(int64_t)r * ldx + c] = x[r][c];
+        Xb[(int64_t)r * ldx + c] = S.x[r][c];
     }
 }
 
@@ -290,11 +164,10 @@ cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, R
 template <typename T>
 cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, int64_t batch, T* Linv,
                           int64_t ldx, int64_t strideX, T* scratch, cudaStream_t s, GemmFn<T> fn, void* fnctx) {
-    auto gemm = [&](GemmProb<T>* p) { return fn ? fn(fnctx, p, 1, s) : gemm_simt<T>(p, 1, s); };
+    auto gemm = [&](GemmProb<T>* p, int np) { return fn ? fn(fnctx, p, np, s) : gemm_simt<T>(p, np, s); };
     if (m <= 0 || batch <= 0) return cudaSuccess;
     cudaError_t err;
-    // Zero the strict upper triangle (and everything else) first; the row
-    // sweep writes only the lower tiles.
+    // Zero everything first: the recursion writes only the lower blocks.
     if (ldx == m && strideX == m * m) {
         err = cudaMemsetAsync(Linv, 0, (size_t)(batch * m * m) * sizeof(T), s);
     } else {
@@ -304,47 +177,62 @@ cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, i
     if (err != cudaSuccess) return err;
     err = trtri_tiles_batched<T>(L, ldl, strideL, (int)m, (int)batch, Linv, ldx, strideX, s);
     if (err != cudaSuccess) return err;
-    for (int64_t r0 = kTile; r0 < m; r0 += kTile) {
-        const int rows = (int)((m - r0) < kTile ? (m - r0) : kTile);
-        // tmp = L[r0:r0+rows, 0:r0] * Linv[0:r0, 0:r0]
-        GemmProb<T> p = blank_prob<T>();
-        p.M = rows;
-        p.N = (int32_t)r0;
-        p.batch = (int32_t)batch;
-        p.nterms = 1;
-        p.term[0].A = L + r0 * ldl;
-        p.term[0].lda = ldl;
-        p.term[0].strideA = strideL;
-        p.term[0].B = Linv;
-        p.term[0].ldb = ldx;
-        p.term[0].strideB = strideX;
-        p.term[0].K = (int32_t)r0;
-        p.term[0].kmode = KM_GE_N0;
-        p.Cout = scratch;
-        p.ldc = m;
-        p.strideC = (int64_t)kTile * m;
-        err = gemm(&p);
-        if (err != cudaSuccess) return err;
-        // Linv[r0:r0+rows, 0:r0] = -Linv[r0:, r0:](tile) * tmp
-        GemmProb<T> q = blank_prob<T>();
-        q.M = rows;
-        q.N = (int32_t)r0;
-        q.batch = (int32_t)batch;
-        q.nterms = 1;
-        q.term[0].A = Linv + r0 * ldx + r0;
-        q.term[0].lda = ldx;
-        q.term[0].strideA = strideX;
-        q.term[0].B = scratch;
-        q.term[0].ldb = m;
-        q.term[0].strideB = (int64_t)kTile * m;
-        q.term[0].K = rows;
-        q.term[0].kmode = KM_LT_M1;
-        q.alpha = T(-1);
-        q.Cout = Linv + r0 * ldx;
-        q.ldc = ldx;
-        q.strideC = strideX;
-        err = gemm(&q);
-        if (err != cudaSuccess) return err;
+    // Recursive doubling: at level h, every pair of h-blocks along the
+    // diagonal, [L11 0; L21 L22], gets X21 = -X22 (L21 X11) from the inverses
+    // X11, X22 of the level below.  Pairs of a level are independent and go
+    // four to a grouped launch; every problem is batched over the blocks.
+    // Scratch per block: the products L21 X11 of one level (<= m*m/2 + h*h).
+    const int64_t sstride = m * m;
+    for (int64_t h = kTile; h < m; h *= 2) {
+        int64_t q = 0;
+        while ((2 * q + 1) * h < m) {
+            GemmProb<T> pr[4], pq[4];
+            int np = 0;
+            for (; np < 4 && (2 * q + 1) * h < m; ++np, ++q) {
+                const int64_t r1 = (2 * q + 1) * h, c0 = 2 * q * h;
+                const int64_t rows2 = (m - r1) < h ? (m - r1) : h;
+                T* tq = scratch + q * h * h;
+                GemmProb<T> p = blank_prob<T>();  // T = L21 X11
+                p.M = (int32_t)rows2;
+                p.N = (int32_t)h;
+                p.batch = (int32_t)batch;
+                p.nterms = 1;
+                p.term[0].A = L + r1 * ldl + c0;
+                p.term[0].lda = ldl;
+                p.term[0].strideA = strideL;
+                p.term[0].B = Linv + c0 * ldx + c0;
+                p.term[0].ldb = ldx;
+                p.term[0].strideB = strideX;
+                p.term[0].K = (int32_t)h;
+                p.term[0].kmode = KM_GE_N0;
+                p.Cout = tq;
+                p.ldc = h;
+                p.strideC = sstride;
+                pr[np] = p;
+                GemmProb<T> w = blank_prob<T>();  // X21 = -X22 T
+                w.M = (int32_t)rows2;
+                w.N = (int32_t)h;
+                w.batch = (int32_t)batch;
+                w.nterms = 1;
+                w.term[0].A = Linv + r1 * ldx + r1;
+                w.term[0].lda = ldx;
+                w.term[0].strideA = strideX;
+                w.term[0].B = tq;
+                w.term[0].ldb = h;
+                w.term[0].strideB = sstride;
+                w.term[0].K = (int32_t)rows2;
+                w.term[0].kmode = KM_LT_M1;
+                w.alpha = T(-1);
+                w.Cout = Linv + r1 * ldx + c0;
+                w.ldc = ldx;
+                w.strideC = strideX;
+                pq[np] = w;
+            }
+            err = gemm(pr, np);
+            if (err != cudaSuccess) return err;
+            err = gemm(pq, np);
+            if (err != cudaSuccess) return err;
+        }
     }
     return cudaSuccess;
 }
