@@ -163,7 +163,7 @@ size_t sgb_pobtaf_noalloc_scratch_bytes(void);
  * dense product every block step of the reference performs with `@`).
  * precision SGB_PREC_NATIVE runs on the FP64 pipe; SGB_PREC_MIXED runs the
  * tensor-core slice products (slice count in bits 8-15 of precision, 3..7,
- * default 5).  transA/transB are 'N' or 'T'.  The first 4 bytes of the
+ * default 6).  transA/transB are 'N' or 'T'.  The first 4 bytes of the
  * workspace receive a device status word (0, or SGB_ERR_TIMEOUT).
  */
 int sgb_dgemm_workspace_size(int precision, int64_t M, int64_t N, int64_t K, size_t* bytes);

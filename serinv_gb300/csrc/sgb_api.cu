@@ -167,7 +167,7 @@ struct PobtafWs {
         Carve c;
         status = c.take(256);
         bar = c.take(256);
-        tinv = c.take(sizeof(T) * kTile * kTile);
+        tinv = c.take(sizeof(T) * (4 * kTile * kTile + 2 * kTile));  // column-block kernel scratch
         const int64_t mx = m->b > m->a ? m->b : m->a;
         tc_bytes = 0;
         if (S) {
@@ -182,29 +182,49 @@ struct PobtafWs {
     }
 };
 
+// pobtasi works through the blocks in chunks: L_jj^{-1}, G_j = Lo_j L_jj^{-1},
+// H_j = Ar_j L_jj^{-1} and P_j = L_jj^{-T} L_jj^{-1} of a chunk are formed
+// by batched products first, then the chunk's back-sweep steps run.
+constexpr int64_t kSiChunk = 64;
+// Blocks per grouped tensor-core launch of those batched products (bounds
+// the slice scratch).
+constexpr int64_t kSiTcBatch = 16;
+
+// Slice scratch gemm_tc takes for one problem (sizes as gemm_tc pads them).
+size_t tc_prob_bytes(int S, int64_t M, int64_t N, int64_t Kpad, int64_t batch) {
+    const int64_t Mpad = ceil_div(M, 128) * 128, Npad = ceil_div(N, kTcBN) * kTcBN;
+    const int64_t Kal = Kpad <= 0 ? 32 : ceil_div(Kpad, 32) * 32;
+    const size_t per = (size_t)S * (Mpad + Npad) * Kal * 2 + (size_t)(Mpad + Npad) * 4;
+    return (per + 255) / 256 * 256 * (size_t)batch + 256;
+}
+
 template <typename T>
 struct PobtasiWs {
-    size_t status, linv, linv_tip, trtri, uv, xt, w, tc, tc_bytes, total;
+    size_t status, linv, linv_tip, trtri, gh, tc, tc_bytes, total;
+    int64_t chunk;
     PobtasiWs(const sgb_bta* m, int S = 0) {
-        const size_t n = m->n, b = m->b, a = m->a;
-        const size_t mx = b > a ? b : a;
+        const int64_t n = m->n, b = m->b, a = m->a;
+        chunk = n < kSiChunk ? (n > 0 ? n : 1) : kSiChunk;
         Carve c;
         status = c.take(256);
         tc_bytes = 0;
         if (S) {
-            const size_t g = tc_bound(S, (int64_t)mx, (int64_t)(b + a), 3);
-            const int64_t chunk = (int64_t)n < kTrtriChunk ? (int64_t)n : kTrtriChunk;
-            const size_t t1 = trtri_tc_bytes(S, (int64_t)b, chunk), t2 = trtri_tc_bytes(S, (int64_t)a, 1);
-            tc_bytes = g > t1 ? g : t1;
-            tc_bytes = tc_bytes > t2 ? tc_bytes : t2;
+            const int64_t kba = ceil_div(b, 32) * 32 + ceil_div(a, 32) * 32;
+            const int64_t tb = chunk < kSiTcBatch ? chunk : kSiTcBatch;
+            size_t need[5];
+            need[0] = tc_prob_bytes(S, b, b, kba, 1) + tc_prob_bytes(S, a, b, kba, 1);  // back-sweep step
+            need[1] = 2 * tc_prob_bytes(S, b, b, b, tb) + tc_prob_bytes(S, a, b, b, tb);  // G, P, H
+            need[2] = trtri_tc_bytes(S, b, chunk);
+            need[3] = trtri_tc_bytes(S, a, 1);
+            need[4] = tc_prob_bytes(S, a, a, a, 1);  // tip
+            for (size_t v : need) tc_bytes = v > tc_bytes ? v : tc_bytes;
         }
         tc = c.take(tc_bytes);
-        linv = c.take(sizeof(T) * n * b * b);
-        linv_tip = c.take(sizeof(T) * a * a);
-        trtri = c.take(sizeof(T) * (trtri_scratch_elems((int64_t)mx, (int64_t)n)));
-        uv = c.take(sizeof(T) * (b + a) * b);
-        xt = c.take(sizeof(T) * (b + a) * b);
-        w = c.take(sizeof(T) * b * b);
+        linv = c.take(sizeof(T) * (size_t)(chunk * b * b));
+        linv_tip = c.take(sizeof(T) * (size_t)(a * a));
+        const size_t t1 = trtri_scratch_elems(b, chunk), t2 = trtri_scratch_elems(a, 1);
+        trtri = c.take(sizeof(T) * (t1 > t2 ? t1 : t2));
+        gh = c.take(sizeof(T) * (size_t)(chunk * (b + a) * b));
         total = c.off;
     }
 };
@@ -306,7 +326,8 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
         if (S == 0 || !kMixedInverseTrsm) {
             cudaError_t e = persistent
                                 ? factor_panel_persistent<T>(Di, b, b, r1, r2, tinv, bar, cx.status, info, i * b, s)
-                                : factor_column_block<T>(Di, b, b, r1, r2, tinv, info, i * b, s);
+                                : cudaErrorNotSupported;
+            if (e == cudaErrorNotSupported) e = factor_column_block<T>(Di, b, b, r1, r2, tinv, info, i * b, s);
             return e == cudaSuccess ? SGB_OK : cuda_fail(e);
         }
         RowSet<T> none{nullptr, 0, b};
@@ -404,6 +425,16 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
 //   X_Lo = U L_ii^{-1} ; X_A = V L_ii^{-1}
 //   X_D  = (L_ii^{-T} - X_Lo^T Lo_i - X_A^T Ar_i) L_ii^{-1}                  (:167-172)
 // The last block (:114-139) is the same step without the i+1 terms.
+// Selected inversion, src/serinv/algs/pobtasi.py:92-172, rearranged so that
+// the back-sweep chain is two grouped products per block.  With
+// G_i = Lo_i L_ii^{-1}, H_i = Ar_i L_ii^{-1}, P_i = L_ii^{-T} L_ii^{-1}
+// (batched over a chunk of blocks, off the chain) the reference's updates
+// (:150-169) read
+//   [X_{i+1,i}; X_{A,i}] = -[X_{i+1,i+1} X_{A,i+1}^T; X_{A,i+1} X_T] [G_i; H_i]
+//   X_{i,i}              = P_i - X_{i+1,i}^T G_i - X_{A,i}^T H_i
+// and the last block (:121-137) is the same without the i+1 terms.  L_ii,
+// Lo_i and Ar_i are dead once G_i, H_i, P_i exist, so P_i is formed in the
+// diagonal block itself and the outputs overwrite the factor in place.
 template <typename T>
 int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaStream_t s) {
     const int64_t n = m->n, b = m->b, a = m->a;
@@ -421,13 +452,8 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
     T* Linv = (T*)(base + W.linv);
     T* Ltinv = (T*)(base + W.linv_tip);
     T* trs = (T*)(base + W.trtri);
-    T* UV = (T*)(base + W.uv);
-    T* XT = (T*)(base + W.xt);
-    T* Wm = (T*)(base + W.w);
-    const int64_t bb = b * b, ab = a * b;
-
-    const int64_t ninv = invert_last_block ? n : n - 1;
-    SGB_TRY(trtri_run<T>(cx, D, b, ninv, Linv, trs, s));
+    T* GH = (T*)(base + W.gh);
+    const int64_t bb = b * b, ab = a * b, ghs = (b + a) * b;
 
     if (invert_last_block && a) {
         // X_T = L_T^{-T} L_T^{-1}  (:115-119)
@@ -440,96 +466,102 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
         SGB_TRY(run_gemm<T>(cx, &p, 1, s));
     }
 
-    const int64_t first = invert_last_block ? n - 1 : n - 2;
-    for (int64_t i = first; i >= 0; --i) {
-        const bool has_next = i < n - 1;
-        const T* Li = Linv + i * bb;
-        T* Di = D + i * bb;
-        T* Loi = has_next ? Lo + i * bb : nullptr;
-        T* Ari = a ? Ar + i * ab : nullptr;
-        T* U = UV;
-        T* V = UV + bb;
-        T* XLo = XT;
-        T* XA = XT + bb;
-
-        // (1) U, V
-        GemmProb<T> pr[3];
-        int np = 0;
-        if (has_next) {
+    // blocks whose L_ii is inverted here: all, or all but the last
+    const int64_t ninv = invert_last_block ? n : n - 1;
+    const int64_t tcb = S ? (W.chunk < kSiTcBatch ? W.chunk : kSiTcBatch) : W.chunk;
+    for (int64_t hi = ninv; hi > 0; hi -= W.chunk) {
+        const int64_t lo = hi > W.chunk ? hi - W.chunk : 0;
+        SGB_TRY(trtri_run<T>(cx, D + lo * bb, b, hi - lo, Linv, trs, s));
+        for (int64_t j0 = lo; j0 < hi; j0 += tcb) {
+            const int64_t jn = (hi - j0) < tcb ? (hi - j0) : tcb;
+            const int64_t ng = (j0 + jn <= n - 1) ? jn : (n - 1 - j0);  // blocks with a Lo_j
+            T* Lj = Linv + (j0 - lo) * bb;
+            T* GHj = GH + (j0 - lo) * ghs;
+            GemmProb<T> pr[3];
+            int np = 0;
+            if (ng > 0) {  // G_j = Lo_j L_jj^{-1}
+                GemmProb<T> p = prob<T>();
+                p.M = p.N = (int32_t)b;
+                p.batch = (int32_t)ng;
+                set_term<T>(p, 0, Lo + j0 * bb, b, 0, Lj, b, 0, b, KM_GE_N0);
+                p.term[0].strideA = bb;
+                p.term[0].strideB = bb;
+                p.Cout = GHj;
+                p.ldc = b;
+                p.strideC = ghs;
+                pr[np++] = p;
+            }
+            if (a) {  // H_j = Ar_j L_jj^{-1}
+                GemmProb<T> p = prob<T>();
+                p.M = (int32_t)a;
+                p.N = (int32_t)b;
+                p.batch = (int32_t)jn;
+                set_term<T>(p, 0, Ar + j0 * ab, b, 0, Lj, b, 0, b, KM_GE_N0);
+                p.term[0].strideA = ab;
+                p.term[0].strideB = bb;
+                p.Cout = GHj + bb;
+                p.ldc = b;
+                p.strideC = ghs;
+                pr[np++] = p;
+            }
+            {  // P_j = L_jj^{-T} L_jj^{-1} into D_j
+                GemmProb<T> p = prob<T>();
+                p.M = p.N = (int32_t)b;
+                p.batch = (int32_t)jn;
+                set_term<T>(p, 0, Lj, b, 1, Lj, b, 0, b, KM_GE_M0);
+                p.term[0].strideA = bb;
+                p.term[0].strideB = bb;
+                p.Cout = D + j0 * bb;
+                p.ldc = b;
+                p.strideC = bb;
+                pr[np++] = p;
+            }
+            SGB_TRY(run_gemm<T>(cx, pr, np, s));
+        }
+        for (int64_t i = hi - 1; i >= lo; --i) {
+            const bool has_next = i < n - 1;
+            const T* G = GH + (i - lo) * ghs;
+            const T* H = G + bb;
+            GemmProb<T> pr[2];
+            int np = 0;
+            if (has_next) {  // X_{i+1,i} = -(X_{i+1,i+1} G_i + X_{A,i+1}^T H_i)  (:150-155)
+                GemmProb<T> p = prob<T>();
+                p.M = p.N = (int32_t)b;
+                set_term<T>(p, 0, D + (i + 1) * bb, b, 0, G, b, 0, b);
+                if (a) set_term<T>(p, 1, Ar + (i + 1) * ab, b, 1, H, b, 0, a);
+                p.alpha = T(-1);
+                p.Cout = Lo + i * bb;
+                p.ldc = b;
+                pr[np++] = p;
+            }
+            if (a) {  // X_{A,i} = -(X_{A,i+1} G_i + X_T H_i)  (:157-162, :128-130)
+                GemmProb<T> p = prob<T>();
+                p.M = (int32_t)a;
+                p.N = (int32_t)b;
+                int t = 0;
+                if (has_next) set_term<T>(p, t++, Ar + (i + 1) * ab, b, 0, G, b, 0, b);
+                set_term<T>(p, t, Tp, a, 0, H, b, 0, a);
+                p.alpha = T(-1);
+                p.Cout = Ar + i * ab;
+                p.ldc = b;
+                pr[np++] = p;
+            }
+            if (np == 0) continue;  // a == 0 and no next block: X_ii = P_i
+            SGB_TRY(run_gemm<T>(cx, pr, np, s));
+            // X_ii = P_i - X_{i+1,i}^T G_i - X_{A,i}^T H_i  (:164-169, :133-137)
             GemmProb<T> p = prob<T>();
             p.M = p.N = (int32_t)b;
-            set_term<T>(p, 0, D + (i + 1) * bb, b, 0, Loi, b, 0, b);
-            if (a) set_term<T>(p, 1, Ar + (i + 1) * ab, b, 1, Ari, b, 0, a);
-            p.alpha = T(-1);
-            p.Cout = U;
-            p.ldc = b;
-            pr[np++] = p;
-        }
-        if (a) {
-            GemmProb<T> p = prob<T>();
-            p.M = (int32_t)a;
-            p.N = (int32_t)b;
             int t = 0;
-            if (has_next) set_term<T>(p, t++, Ar + (i + 1) * ab, b, 0, Loi, b, 0, b);
-            set_term<T>(p, t, Tp, a, 0, Ari, b, 0, a);
-            p.alpha = T(-1);
-            p.Cout = V;
-            p.ldc = b;
-            pr[np++] = p;
-        }
-        if (np) SGB_TRY(run_gemm<T>(cx, pr, np, s));
-
-        // (2) X_Lo = U Linv, X_A = V Linv
-        np = 0;
-        if (has_next) {
-            GemmProb<T> p = prob<T>();
-            p.M = p.N = (int32_t)b;
-            set_term<T>(p, 0, U, b, 0, Li, b, 0, b, KM_GE_N0);
-            p.Cout = XLo;
-            p.ldc = b;
-            pr[np++] = p;
-        }
-        if (a) {
-            GemmProb<T> p = prob<T>();
-            p.M = (int32_t)a;
-            p.N = (int32_t)b;
-            set_term<T>(p, 0, V, b, 0, Li, b, 0, b, KM_GE_N0);
-            p.Cout = XA;
-            p.ldc = b;
-            pr[np++] = p;
-        }
-        if (np) SGB_TRY(run_gemm<T>(cx, pr, np, s));
-
-        // (3) W = Linv^T - X_Lo^T Lo_i - X_A^T Ar_i
-        {
-            GemmProb<T> p = prob<T>();
-            p.M = p.N = (int32_t)b;
-            int t = 0;
-            if (has_next) set_term<T>(p, t++, XLo, b, 1, Loi, b, 0, b);
-            if (a) set_term<T>(p, t++, XA, b, 1, Ari, b, 0, a);
+            if (has_next) set_term<T>(p, t++, Lo + i * bb, b, 1, G, b, 0, b);
+            if (a) set_term<T>(p, t++, Ar + i * ab, b, 1, H, b, 0, a);
             p.alpha = T(-1);
             p.beta = T(1);
-            p.Cin = Li;
+            p.Cin = D + i * bb;
             p.ldcin = b;
-            p.transCin = 1;
-            p.Cout = Wm;
+            p.Cout = D + i * bb;
             p.ldc = b;
             SGB_TRY(run_gemm<T>(cx, &p, 1, s));
         }
-
-        // (4) X_D = W Linv ; Lo_i <- X_Lo ; Ar_i <- X_A
-        np = 0;
-        {
-            GemmProb<T> p = prob<T>();
-            p.M = p.N = (int32_t)b;
-            set_term<T>(p, 0, Wm, b, 0, Li, b, 0, b, KM_GE_N0);
-            p.Cout = Di;
-            p.ldc = b;
-            pr[np++] = p;
-        }
-        if (has_next) pr[np++] = copy_prob<T>(Loi, b, XLo, b, b, b);
-        if (a) pr[np++] = copy_prob<T>(Ari, b, XA, b, a, b);
-        SGB_TRY(run_gemm<T>(cx, pr, np, s));
     }
     return SGB_OK;
 }

@@ -53,7 +53,7 @@ namespace {
 constexpr int TC_BM = 128;
 constexpr int TC_BK = 32;
 constexpr int kMaxTcProbs = 4;
-constexpr int kMaxSplitJobs = 2 * kMaxTcProbs * 2;  // probs x operands x terms
+constexpr int kMaxSplitJobs = 2 * kMaxTcProbs;  // probs x operands
 constexpr long long kSpinLimit = 1ll << 22;         // bounded mbarrier waits (~1 s)
 
 // ---------------------------------------------------------------- split
@@ -65,16 +65,22 @@ struct SplitSrc {
     int32_t K, koff;      // source K extent; destination K offset (multiple of TC_BK)
 };
 
+// One operand of one problem: the rows of op(A) (or the columns of op(B))
+// over the K ranges of all its terms.
 struct SplitJob {
-    SplitSrc src;
+    SplitSrc src[2];
+    int32_t nsrc;
     __nv_bfloat16* out;   // per instance: [S][Rpad/RT][Kpad/32] chunks of RT x 32 (core-matrix order)
-    int32_t* exps;        // [Rpad] per instance (biased FP64 exponent of the row max)
+    int32_t* exps;        // [Rpad] per instance (biased FP64 exponent of the row max, 0 for a zero row)
     int64_t out_stride, exp_stride;
     int32_t R, Rpad, Kpad;
     int32_t RT;           // rows per chunk: 128 for A, the tile width for B
     int32_t batch;
-    int32_t tiles_r, tiles_k, tile_begin;
+    int32_t strips, strip_begin;  // kSplitRows-row strips per instance; first CTA of the job
 };
+
+constexpr int kSplitRows = 8;
+constexpr int kSplitLd = kTcMaxK + 1;  // odd stride: conflict-free row and column access
 
 struct SplitLaunch {
     SplitJob j[kMaxSplitJobs];
@@ -82,55 +88,12 @@ struct SplitLaunch {
     int32_t S;
 };
 
-__device__ __forceinline__ int find_job(const SplitLaunch& L, int tile) {
+__device__ __forceinline__ int find_job(const SplitLaunch& L, int cta) {
     int ji = 0;
 #pragma unroll 1
     for (int q = 1; q < L.nj; ++q)
-        if (tile >= L.j[q].tile_begin) ji = q;
+        if (cta >= L.j[q].strip_begin) ji = q;
     return ji;
-}
-
-// Load a 32 x 32 tile of the source into shared memory, coalesced along
-// whichever index is contiguous.  Elements outside the source are zero.
-__device__ __forceinline__ void load_tile(const SplitJob& J, int inst, int r0, int k0, double (*t)[33]) {
-    const double* X = J.src.X + (int64_t)inst * J.src.stride;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-    if (J.src.ld_k == 1) {
-        for (int rr = ty; rr < 32; rr += 8) {
-            const int r = r0 + rr, k = k0 + tx;
-            t[rr][tx] = (r < J.R && k < J.src.K) ? X[(int64_t)r * J.src.ld_r + k] : 0.0;
-        }
-    } else {
-        for (int kk = ty; kk < 32; kk += 8) {
-            const int r = r0 + tx, k = k0 + kk;
-            t[tx][kk] = (r < J.R && k < J.src.K) ? X[(int64_t)r * J.src.ld_r + (int64_t)k * J.src.ld_k] : 0.0;
-        }
-    }
-}
-
-__global__ void __launch_bounds__(256) k_split_exp(const __grid_constant__ SplitLaunch L) {
-    __shared__ double t[32][33];
-    const int tile = blockIdx.x;
-    const SplitJob& J = L.j[find_job(L, tile)];
-    int local = tile - J.tile_begin;
-    const int per = J.tiles_r * J.tiles_k;
-    const int inst = local / per;
-    local -= inst * per;
-    const int r0 = (local / J.tiles_k) * 32;
-    const int k0 = (local % J.tiles_k) * 32;
-    if (k0 >= J.src.K || r0 >= J.R) return;
-    load_tile(J, inst, r0, k0, t);
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        const int rr = threadIdx.x;
-        int emax = 0;
-        for (int kk = 0; kk < 32; ++kk) {
-            const unsigned long long bits = (unsigned long long)__double_as_longlong(t[rr][kk]);
-            const int e = (int)((bits >> 52) & 0x7ff);
-            emax = e > emax ? e : emax;
-        }
-        if (r0 + rr < J.R && emax > 0) atomicMax(J.exps + (int64_t)inst * J.exp_stride + r0 + rr, emax);
-    }
 }
 
 // Balanced base-128 digits of x scaled by the row exponent Erow (biased).
@@ -158,44 +121,85 @@ __device__ __forceinline__ void digits(double x, int Erow, int (&d)[S]) {
     d[0] = (int)X;
 }
 
+// One CTA per strip of kSplitRows rows of one operand instance: the whole
+// strip (all terms, K <= kTcMaxK) is staged in shared memory with coalesced
+// loads, each row's largest exponent is found by one warp, and the S slices
+// of every element are written in the chunk layout the MMA descriptors
+// read -- padding rows and the K padding of each term as zeros, so the
+// buffers need no clearing beforehand.
 template <int S>
-__global__ void __launch_bounds__(256) k_split_slices(const __grid_constant__ SplitLaunch L) {
-    __shared__ double t[32][33];
-    __shared__ int ex[32];
-    const int tile = blockIdx.x;
-    const SplitJob& J = L.j[find_job(L, tile)];
-    int local = tile - J.tile_begin;
-    const int per = J.tiles_r * J.tiles_k;
-    const int inst = local / per;
-    local -= inst * per;
-    const int r0 = (local / J.tiles_k) * 32;
-    const int k0 = (local % J.tiles_k) * 32;  // within this source's padded K range
-    load_tile(J, inst, r0, k0, t);
-    if (threadIdx.x < 32) {
-        const int r = r0 + threadIdx.x;
-        ex[threadIdx.x] = r < J.R ? J.exps[(int64_t)inst * J.exp_stride + r] : 0;
+__global__ void __launch_bounds__(256) k_split(const __grid_constant__ SplitLaunch L) {
+    __shared__ double t[kSplitRows][kSplitLd];
+    __shared__ int ex[kSplitRows];
+    const SplitJob& J = L.j[find_job(L, blockIdx.x)];
+    const int local = blockIdx.x - J.strip_begin;
+    const int inst = local / J.strips;
+    const int r0 = (local - inst * J.strips) * kSplitRows;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < kSplitRows * J.Kpad; e += 256) t[e / J.Kpad][e % J.Kpad] = 0.0;
+    __syncthreads();
+    // Loads are issued kSplitBatch at a time per thread before any is
+    // stored, so a CTA has its whole strip in flight at once.
+    constexpr int kSplitBatch = 6;
+    for (int q = 0; q < J.nsrc; ++q) {
+        const SplitSrc& src = J.src[q];
+        const double* X = src.X + (int64_t)inst * src.stride;
+        const int total = kSplitRows * src.K;
+        const bool rowmajor = src.ld_k == 1;  // else columns contiguous in r
+        for (int e0 = tid; e0 < total; e0 += 256 * kSplitBatch) {
+            double v[kSplitBatch];
+            int dst[kSplitBatch];
+#pragma unroll
+            for (int u = 0; u < kSplitBatch; ++u) {
+                const int e = e0 + u * 256;
+                int rr, k;
+                if (rowmajor) {  // a warp reads 32 consecutive k of one row
+                    rr = e / src.K;
+                    k = e - rr * src.K;
+                } else {  // eight rows of four k per warp
+                    k = e / kSplitRows;
+                    rr = e % kSplitRows;
+                }
+                const int r = r0 + rr;
+                const bool in = e < total && r < J.R;
+                dst[u] = in ? rr * kSplitLd + src.koff + k : -1;
+                v[u] = in ? __ldg(X + (int64_t)r * src.ld_r + (int64_t)k * src.ld_k) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kSplitBatch; ++u)
+                if (dst[u] >= 0) (&t[0][0])[dst[u]] = v[u];
+        }
     }
     __syncthreads();
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int warp = tid >> 5, lane = tid & 31;
+    if (warp < kSplitRows) {
+        int emax = 0;
+        for (int k = lane; k < J.Kpad; k += 32) {
+            const int e = (int)(((unsigned long long)__double_as_longlong(t[warp][k]) >> 52) & 0x7ff);
+            emax = e > emax ? e : emax;
+        }
+        emax = __reduce_max_sync(0xffffffffu, emax);
+        if (lane == 0) {
+            ex[warp] = emax;
+            J.exps[(int64_t)inst * J.exp_stride + r0 + warp] = emax;
+        }
+    }
+    __syncthreads();
     __nv_bfloat16* out = J.out + (int64_t)inst * J.out_stride;
     const int64_t slice = (int64_t)J.Rpad * J.Kpad;
     const int nkb = J.Kpad / 32, RT = J.RT;
-    const int kb = (J.src.koff + k0) / 32;  // k within the block = tx
-    for (int rr = ty; rr < 32; rr += 8) {
+    for (int e = tid; e < kSplitRows * J.Kpad; e += 256) {
+        const int rr = e % kSplitRows, k = e / kSplitRows;
         const int r = r0 + rr;
-        if (r >= J.Rpad) continue;
         int d[S];
-        digits<S>(t[rr][tx], ex[rr], d);
-        // chunk (r / RT, kb) of RT x 32 elements in core-matrix order:
+        digits<S>(t[rr][k], ex[rr], d);
+        // chunk (r / RT, k / 32) of RT x 32 elements in core-matrix order:
         // [k/8][row/8][row%8][k%8]
-        const int rt = r / RT, ri = r % RT;
-        const int64_t o = ((int64_t)rt * nkb + kb) * (RT * 32) + ((tx >> 3) * (RT >> 3) + (ri >> 3)) * 64 +
-                          (ri & 7) * 8 + (tx & 7);
+        const int rt = r / RT, ri = r % RT, kb = k >> 5, kk = k & 31;
+        const int64_t o = ((int64_t)rt * nkb + kb) * (RT * 32) + ((kk >> 3) * (RT >> 3) + (ri >> 3)) * 64 +
+                          (ri & 7) * 8 + (kk & 7);
 #pragma unroll
-        for (int p = 0; p < S; ++p) {
-            const float w = ldexpf((float)d[p], -7 * p);
-            out[p * slice + o] = __float2bfloat16_rn(w);
-        }
+        for (int p = 0; p < S; ++p) out[p * slice + o] = __float2bfloat16_rn(ldexpf((float)d[p], -7 * p));
     }
 }
 
@@ -606,16 +610,13 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
     TL.err = err;
     char* base = (char*)ws;
     size_t off = 0;
-    int64_t split_tiles = 0, gemm_tiles = 0;
+    int64_t split_ctas = 0, gemm_tiles = 0;
     // 128 x 64 tiles unless that leaves most SMs idle; then 128 x 32.
     int64_t tiles64 = 0;
     for (int i = 0; i < np; ++i)
         if (probs[i].M > 0 && probs[i].N > 0 && probs[i].batch > 0)
             tiles64 += ceil_div(probs[i].M, TC_BM) * ceil_div(probs[i].N, kTcBN) * probs[i].batch;
     const int bn = tiles64 < 148 ? 32 : 64;
-    struct ExpRange { int32_t* p; size_t bytes; };
-    ExpRange ranges[kMaxTcProbs * 2];
-    int nranges = 0;
     for (int i = 0; i < np; ++i) {
         const GemmProb<double>& p = probs[i];
         if (p.M <= 0 || p.N <= 0 || p.batch <= 0) continue;
@@ -633,53 +634,56 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
         __nv_bfloat16* Bs = (__nv_bfloat16*)(base + off + bytesA);
         int32_t* eA = (int32_t*)(base + off + bytesA + bytesB);
         int32_t* eB = eA + Mpad;
-        ranges[nranges++] = ExpRange{eA, 0};
-        // exps live inside each instance block; zero them per instance below
         const int64_t inst_stride_bytes = (int64_t)per_al;
-        // split jobs: one per (operand, term)
+        // split jobs: op(A) rows and op(B) columns, all terms
+        SplitJob ja, jb;
+        memset(&ja, 0, sizeof(ja));
+        memset(&jb, 0, sizeof(jb));
         int32_t koff = 0;
         for (int t = 0; t < p.nterms; ++t) {
             const GemmTerm<double>& tm = p.term[t];
             if (tm.K <= 0) continue;
-            // op(A_t): row m, column k
-            SplitJob ja;
-            memset(&ja, 0, sizeof(ja));
-            ja.src.X = tm.A;
-            ja.src.ld_r = tm.transA ? 1 : tm.lda;
-            ja.src.ld_k = tm.transA ? tm.lda : 1;
-            ja.src.stride = tm.strideA;
-            ja.src.K = tm.K;
-            ja.src.koff = koff;
-            ja.out = As;
-            ja.exps = eA;
-            ja.out_stride = inst_stride_bytes / 2;
-            ja.exp_stride = inst_stride_bytes / 4;
-            ja.R = p.M;
-            ja.Rpad = (int32_t)Mpad;
-            ja.RT = TC_BM;
-            ja.Kpad = (int32_t)Kalloc;
-            ja.batch = p.batch;
-            ja.tiles_r = (int32_t)ceil_div(Mpad, 32);
-            ja.tiles_k = (int32_t)ceil_div(tm.K, TC_BK);
-            // op(B_t): row n (column of op(B)), column k
-            SplitJob jb = ja;
-            jb.src.X = tm.B;
-            jb.src.ld_r = tm.transB ? tm.ldb : 1;
-            jb.src.ld_k = tm.transB ? 1 : tm.ldb;
-            jb.src.stride = tm.strideB;
-            jb.out = Bs;
-            jb.exps = eB;
-            jb.R = p.N;
-            jb.Rpad = (int32_t)Npad;
-            jb.RT = bn;
-            jb.tiles_r = (int32_t)ceil_div(Npad, 32);
-            for (SplitJob* j : {&ja, &jb}) {
-                if (SL.nj >= kMaxSplitJobs) return cudaErrorInvalidValue;
-                j->tile_begin = (int32_t)split_tiles;
-                split_tiles += (int64_t)j->tiles_r * j->tiles_k * j->batch;
-                SL.j[SL.nj++] = *j;
-            }
+            SplitSrc& sa = ja.src[ja.nsrc++];
+            sa.X = tm.A;
+            sa.ld_r = tm.transA ? 1 : tm.lda;
+            sa.ld_k = tm.transA ? tm.lda : 1;
+            sa.stride = tm.strideA;
+            sa.K = tm.K;
+            sa.koff = koff;
+            SplitSrc& sb = jb.src[jb.nsrc++];
+            sb.X = tm.B;
+            sb.ld_r = tm.transB ? tm.ldb : 1;
+            sb.ld_k = tm.transB ? 1 : tm.ldb;
+            sb.stride = tm.strideB;
+            sb.K = tm.K;
+            sb.koff = koff;
             koff += (int32_t)(ceil_div(tm.K, TC_BK) * TC_BK);
+        }
+        ja.out = As;
+        ja.exps = eA;
+        ja.out_stride = inst_stride_bytes / 2;
+        ja.exp_stride = inst_stride_bytes / 4;
+        ja.R = p.M;
+        ja.Rpad = (int32_t)Mpad;
+        ja.RT = TC_BM;
+        ja.Kpad = (int32_t)Kalloc;
+        ja.batch = p.batch;
+        ja.strips = (int32_t)(Mpad / kSplitRows);
+        jb.out = Bs;
+        jb.exps = eB;
+        jb.out_stride = ja.out_stride;
+        jb.exp_stride = ja.exp_stride;
+        jb.R = p.N;
+        jb.Rpad = (int32_t)Npad;
+        jb.RT = bn;
+        jb.Kpad = (int32_t)Kalloc;
+        jb.batch = p.batch;
+        jb.strips = (int32_t)(Npad / kSplitRows);
+        for (SplitJob* j : {&ja, &jb}) {
+            if (SL.nj >= kMaxSplitJobs) return cudaErrorInvalidValue;
+            j->strip_begin = (int32_t)split_ctas;
+            split_ctas += (int64_t)j->strips * j->batch;
+            SL.j[SL.nj++] = *j;
         }
         TcProb tp;
         memset(&tp, 0, sizeof(tp));
@@ -710,28 +714,17 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
         tp.tile_begin = (int32_t)gemm_tiles;
         gemm_tiles += (int64_t)tp.tiles_m * tp.tiles_n * p.batch;
         TL.p[TL.np++] = tp;
-        // the whole instance block (slices + exps) is zeroed: padding slices
-        // beyond the sources and the exponent maxima must start at zero
-        ranges[nranges - 1].bytes = per_al * p.batch;
-        ranges[nranges - 1].p = (int32_t*)As;
         off += per_al * p.batch;
     }
     if (TL.np == 0) return cudaSuccess;
-    for (int r = 0; r < nranges; ++r) {
-        cudaError_t e = cudaMemsetAsync(ranges[r].p, 0, ranges[r].bytes, s);
-        if (e != cudaSuccess) return e;
-    }
-    if (split_tiles > 0) {
-        prof_before(s);
-        k_split_exp<<<(unsigned)split_tiles, 256, 0, s>>>(SL);
-        prof_after(SGB_KCLASS_SPLIT, s, 0.0);
+    if (split_ctas > 0) {
         prof_before(s);
         switch (S) {
-            case 3: k_split_slices<3><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
-            case 4: k_split_slices<4><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
-            case 5: k_split_slices<5><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
-            case 6: k_split_slices<6><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
-            default: k_split_slices<7><<<(unsigned)split_tiles, 256, 0, s>>>(SL); break;
+            case 3: k_split<3><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
+            case 4: k_split<4><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
+            case 5: k_split<5><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
+            case 6: k_split<6><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
+            default: k_split<7><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
         }
         prof_after(SGB_KCLASS_SPLIT, s, 0.0);
         cudaError_t e = cudaGetLastError();

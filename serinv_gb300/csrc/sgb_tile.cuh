@@ -38,7 +38,9 @@ struct Smem {
     T s[kTile][kTile + 1];
     T x[kTile][kTile + 1];
     T tmp[kTile][kTile + 1];
+    T u[kTile][kTile + 1];
     T yv[kTile];
+    unsigned short tri[kTile * (kTile + 1) / 2];  // (row << 8) | col of the lower triangle, row-major
     int fail;
     int flag;
 };
@@ -103,57 +105,302 @@ __device__ void tile_inverse_dev(Smem<T>& S) {
     }
 }
 
-// A(p): Cholesky + inverse of the diagonal tile at `tile` (nb <= 32), by one CTA.
+// Reciprocal of a positive, normal pivot with the FP64 chain cut to three
+// dependent instructions: a 20-bit seed from the FP32 approximate
+// reciprocal of the mantissa (exponent handled on the bits), then the
+// truncated series 1/d = r0 (1 + e + e^2 + ...), e = 1 - d r0 (Markstein /
+// Goldschmidt refinement), whose e^3 ~ 2^-60 term is below half an ulp.
+// Pivots too large for the exponent trick (d >= 2^1021) take the IEEE
+// division; the branch is uniform because every lane holds the same pivot.
+__device__ __forceinline__ double rcp_pivot(double d) {
+    const int hi = __double2hiint(d);
+    const int E = (hi >> 20) & 0x7ff;
+    if (E > 2044) return 1.0 / d;
+    const float mf = __int_as_float(0x3f800000 | ((hi & 0xfffff) << 3));
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(mf));
+    const int rb = __float_as_int(rf);
+    const int ebits = ((rb >> 23) & 0xff) - 127 - (E - 1023) + 1023;
+    const int mant = rb & 0x7fffff;
+    const double r0 = __hiloint2double((ebits << 20) | (mant >> 3), (mant & 7) << 29);
+    const double e = fma(-d, r0, 1.0);
+    const double t = fma(e, e, e);
+    return fma(r0, t, r0);
+}
+__device__ __forceinline__ float rcp_pivot(float d) { return 1.0f / d; }
+
+// Named barriers of the pivot/worker pipeline (ids 1-4; 0 is __syncthreads).
+__device__ __forceinline__ void nbar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void nbar_arrive(int id, int n) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// Unit-lower inverse Z = M^{-1} from its 8 x 8 diagonal blocks (already in
+// z) by recursive doubling, 8 -> 16 -> 32: Z21 = -Z22 (M21 Z11).  M's strict
+// lower part is in m (unit diagonal implied), u is scratch.
+template <typename T>
+__device__ void unit_inverse_doubling(T (*m)[kTile + 1], T (*z)[kTile + 1], T (*u)[kTile + 1]) {
+    const int tid = threadIdx.x;
+#pragma unroll 1
+    for (int h = 8; h < kTile; h *= 2) {
+        const int nout = (kTile / (2 * h)) * h * h;  // 128, then 256
+        int r = 0, c = 0, o = 0;
+        const bool act = tid < nout;
+        if (act) {
+            const int bi = tid / (h * h), rem = tid % (h * h);
+            r = rem / h;
+            c = rem % h;
+            o = bi * 2 * h;
+            // u = M21 Z11, Z11 unit lower: k >= c, Z11(c, c) = 1
+            const T* mr = &m[o + h + r][o];
+            T a0 = mr[c], a1 = T(0), a2 = T(0), a3 = T(0);
+            int k = c + 1;
+            for (; k + 3 < h; k += 4) {
+                a0 = fma(mr[k], z[o + k][o + c], a0);
+                a1 = fma(mr[k + 1], z[o + k + 1][o + c], a1);
+                a2 = fma(mr[k + 2], z[o + k + 2][o + c], a2);
+                a3 = fma(mr[k + 3], z[o + k + 3][o + c], a3);
+            }
+            for (; k < h; ++k) a0 = fma(mr[k], z[o + k][o + c], a0);
+            u[o + h + r][o + c] = (a0 + a1) + (a2 + a3);
+        }
+        __syncthreads();
+        if (act) {
+            // Z21 = -Z22 u, Z22 unit lower: k <= r, Z22(r, r) = 1
+            const T* zr = &z[o + h + r][o + h];
+            T a0 = u[o + h + r][o + c], a1 = T(0), a2 = T(0), a3 = T(0);
+            int k = 0;
+            for (; k + 3 < r; k += 4) {
+                a0 = fma(zr[k], u[o + h + k][o + c], a0);
+                a1 = fma(zr[k + 1], u[o + h + k + 1][o + c], a1);
+                a2 = fma(zr[k + 2], u[o + h + k + 2][o + c], a2);
+                a3 = fma(zr[k + 3], u[o + h + k + 3][o + c], a3);
+            }
+            for (; k < r; ++k) a0 = fma(zr[k], u[o + h + k][o + c], a0);
+            z[o + h + r][o + c] = -((a0 + a1) + (a2 + a3));
+        }
+        __syncthreads();
+    }
+}
+
+// Cholesky + inverse of the diagonal tile at `tile` (nb <= 32), by one CTA,
+// as L = M D^{1/2} (M unit lower, D the pivots) so that the sequential
+// chain carries no square root:
+//
+// * the pivot warp (warp 0) produces column j: it applies the update of
+//   column j-1 (held in its registers), reads the pivot d_j, forms 1/d_j
+//   and M(:, j) = a'(:, j) / d_j, and publishes both (named barrier READY);
+//   per column that is five FP64 instructions on its SM quarter, which no
+//   other warp shares (warp 4 stays idle);
+// * six worker warps (quarters 1-3) follow one column behind: with column
+//   k they apply the rank-1 update to columns k+2.. (the pivot warp does
+//   column k+1 itself), one triangle element per thread from a packed
+//   index table, and advance the inverse of M's 8 x 8 diagonal blocks by
+//   one row (Z(k, :) = -acc(k, :), acc(i, :) += M(i, k) Z(k, :) for i > k
+//   in k's block), then signal UPD; the pivot warp waits for UPD(j-2)
+//   before column j;
+// * READY and UPD alternate between two barrier ids each, so neither side
+//   can run two generations ahead of the other;
+// * afterwards recursive doubling completes Z = M^{-1}, and
+//   L = a' diag(d)^{-1/2}, L^{-1} = diag(d)^{-1/2} Z.
 template <typename T>
 __device__ void factor_tile(Smem<T>& S, T* tile, int64_t ld, int nb, int zero_right, T* tinv, int32_t* info,
                             int64_t row0) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    constexpr int kPipe = 32 + 192;  // pivot warp + worker warps
     for (int e = tid; e < kTile * kTile; e += kTileThreads) {
         const int r = e / kTile, c = e % kTile;
         T v = T(0);
         if (r < nb && c <= r) v = __ldcg(tile + (int64_t)r * ld + c);
         else if (r >= nb && r == c) v = T(1);
         S.s[r][c] = v;
+        S.tmp[r][c] = T(0);  // inverse accumulators
+        S.x[r][c] = T(0);
+        if (c <= r) S.tri[r * (r + 1) / 2 + c] = (unsigned short)((r << 8) | c);
     }
     if (tid == 0) S.fail = 0;
-    if (tid < kTile) S.yv[tid] = T(1);
     __syncthreads();
-    const int wk = warp == 0 || warp == 4 ? -1 : (warp < 4 ? warp - 1 : warp - 2);
-    for (int j = 0; j < nb; ++j) {
-        if (warp == 0) {
-            const T d = S.s[j][j];
-            const bool bad = !pivot_ok(d);
-            const T y = bad ? T(NAN) : rsq<T>(d);
-            if (lane > j && lane < nb) S.s[lane][j] *= y;
+    if (warp == 0) {
+        T prev_a = T(0), prev_m = T(0);
+        for (int j = 0; j < nb; ++j) {
+            if (j >= 2) nbar_sync(3 + (j & 1), kPipe);  // UPD(j-2)
+            T col = S.s[lane][j];
+            if (j >= 1) col = fma(-prev_a, __shfl_sync(0xffffffffu, prev_m, j), col);
+            const T d = __shfl_sync(0xffffffffu, col, j);
+            const bool ok = pivot_ok(d);
+            const T inv = ok ? rcp_pivot(d) : T(NAN);
+            const T mcol = col * inv;
+            if (lane >= j) S.s[lane][j] = col;
+            if (lane > j) S.x[lane][j] = mcol;
             if (lane == j) {
-                S.s[j][j] = d * y;
-                S.yv[j] = y;
-                if (bad && S.fail == 0) S.fail = j + 1;
+                S.yv[j] = d;
+                if (!ok && S.fail == 0) S.fail = j + 1;
             }
-        } else if (wk >= 0 && j >= 1) {
-            const int c0 = j + 1, k = j - 1, w = nb - c0;
-            for (int e = wk * 32 + lane; e < w * w; e += 6 * 32) {
-                const int rr = c0 + e / w, cc = c0 + e % w;
-                if (cc <= rr) S.s[rr][cc] = fma(-S.s[rr][k], S.s[cc][k], S.s[rr][cc]);
-            }
+            nbar_arrive(1 + (j & 1), kPipe);  // READY(j)
+            prev_a = col;
+            prev_m = mcol;
         }
-        __syncthreads();
-        if (warp == 0 && j + 1 < nb && lane >= j + 1 && lane < nb)
-            S.s[lane][j + 1] = fma(-S.s[lane][j], S.s[j + 1][j], S.s[lane][j + 1]);
+    } else if (warp != 4) {
+        const int wid = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;  // 0..191
+        for (int k = 0; k < nb; ++k) {
+            nbar_sync(1 + (k & 1), kPipe);  // READY(k)
+            const int w = nb - k - 2;
+            const int n1 = w > 0 ? w * (w + 1) / 2 : 0;
+            const int kb = k & ~7, kl = k - kb;
+            const int ibe = (kb + 8 < nb ? kb + 8 : nb);  // end of k's 8-block
+            const int n2 = (ibe - k - 1) * (kl + 1);
+            for (int e = wid; e < n1 + n2; e += 192) {
+                if (e < n1) {  // trailing rank-1 update of columns k+2..
+                    const int rc = S.tri[e];
+                    const int r = k + 2 + (rc >> 8), c = k + 2 + (rc & 0xff);
+                    S.s[r][c] = fma(-S.s[r][k], S.x[c][k], S.s[r][c]);
+                } else {  // inverse of k's 8-block: acc(i, c) += M(i, k) Z(k, c)
+                    const int f = e - n1;
+                    const int i = k + 1 + f / (kl + 1), c = kb + f % (kl + 1);
+                    const T zk = (c == k) ? T(1) : -S.tmp[k][c];
+                    S.tmp[i][c] = fma(S.x[i][k], zk, S.tmp[i][c]);
+                }
+            }
+            if (k + 2 < nb) nbar_arrive(3 + (k & 1), kPipe);  // UPD(k)
+        }
     }
     __syncthreads();
+    for (int e = tid; e < kTile * kTile; e += kTileThreads) {  // Z's 8-blocks from the accumulators
+        const int r = e / kTile, c = e % kTile;
+        S.tmp[r][c] = (r == c) ? T(1) : -S.tmp[r][c];
+    }
+    if (tid < kTile) {
+        const T d = S.yv[tid];
+        S.yv[tid] = (tid < nb) ? rsq<T>(d) : T(1);
+        S.u[tid][tid] = (tid < nb) ? d : T(1);  // pivot, read back below
+    }
+    __syncthreads();
+    unit_inverse_doubling<T>(S.x, S.tmp, S.u);  // leaves the diagonal of u alone
     if (tid == 0 && S.fail != 0 && info != nullptr) atomicCAS(info, 0, (int32_t)(row0 + S.fail));
-    tile_inverse_dev<T>(S);
-    for (int e = tid; e < nb * nb; e += kTileThreads) {
-        const int r = e / nb, c = e % nb;
-        tile[(int64_t)r * ld + c] = (c <= r) ? S.s[r][c] : T(0);
-        tinv[r * kTile + c] = S.x[r][c];
+    for (int e = tid; e < kTile * kTile; e += kTileThreads) {
+        const int r = e / kTile, c = e % kTile;
+        T lv = T(0), xv = T(0);
+        if (c < r) {
+            lv = S.s[r][c] * S.yv[c];
+            xv = S.tmp[r][c] * S.yv[r];
+        } else if (c == r) {
+            lv = S.u[r][r] * S.yv[r];
+            xv = S.yv[r];
+        }
+        if (r < nb && c < nb) {
+            tile[(int64_t)r * ld + c] = lv;
+            tinv[r * kTile + c] = xv;
+        }
+        S.s[r][c] = lv;
+        S.x[r][c] = xv;
     }
     for (int e = tid; e < nb * zero_right; e += kTileThreads) {
         const int r = e / zero_right, c = e % zero_right;
         tile[(int64_t)r * ld + nb + c] = T(0);
     }
+    __syncthreads();
 }
 
+// The pipeline part of factor_tile alone: after it, S.x holds the strict
+// lower part of M (zero elsewhere) and S.yv the pivots d (1 beyond nb), so
+// L = M diag(d)^{1/2}.  No inverse, no output: the persistent column-block
+// kernel publishes M and d and leaves the rest to other CTAs.
+template <typename T>
+__device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int32_t* info, int64_t row0) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    constexpr int kPipe = 32 + 192;
+    for (int e = tid; e < kTile * kTile; e += kTileThreads) {
+        const int r = e / kTile, c = e % kTile;
+        T v = T(0);
+        if (r < nb && c <= r) v = __ldcg(tile + (int64_t)r * ld + c);
+        else if (r >= nb && r == c) v = T(1);
+        S.s[r][c] = v;
+        S.x[r][c] = T(0);
+        if (c <= r) S.tri[r * (r + 1) / 2 + c] = (unsigned short)((r << 8) | c);
+    }
+    if (tid < kTile) S.yv[tid] = T(1);
+    if (tid == 0) S.fail = 0;
+    __syncthreads();
+    if (warp == 0) {
+        T prev_a = T(0), prev_m = T(0);
+        for (int j = 0; j < nb; ++j) {
+            if (j >= 2) nbar_sync(3 + (j & 1), kPipe);  // UPD(j-2)
+            T col = S.s[lane][j];
+            if (j >= 1) col = fma(-prev_a, __shfl_sync(0xffffffffu, prev_m, j), col);
+            const T d = __shfl_sync(0xffffffffu, col, j);
+            const bool ok = pivot_ok(d);
+            const T inv = ok ? rcp_pivot(d) : T(NAN);
+            const T mcol = col * inv;
+            if (lane >= j) S.s[lane][j] = col;
+            if (lane > j) S.x[lane][j] = mcol;
+            if (lane == j) {
+                S.yv[j] = d;
+                if (!ok && S.fail == 0) S.fail = j + 1;
+            }
+            nbar_arrive(1 + (j & 1), kPipe);  // READY(j)
+            prev_a = col;
+            prev_m = mcol;
+        }
+    } else if (warp != 4) {
+        const int wid = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;  // 0..191
+        for (int k = 0; k < nb; ++k) {
+            nbar_sync(1 + (k & 1), kPipe);  // READY(k)
+            const int w = nb - k - 2;
+            const int n1 = w > 0 ? w * (w + 1) / 2 : 0;
+            for (int e = wid; e < n1; e += 192) {  // rank-1 update of columns k+2..
+                const int rc = S.tri[e];
+                const int r = k + 2 + (rc >> 8), c = k + 2 + (rc & 0xff);
+                S.s[r][c] = fma(-S.s[r][k], S.x[c][k], S.s[r][c]);
+            }
+            if (k + 2 < nb) nbar_arrive(3 + (k & 1), kPipe);  // UPD(k)
+        }
+    }
+    __syncthreads();
+    if (tid == 0 && S.fail != 0 && info != nullptr) atomicCAS(info, 0, (int32_t)(row0 + S.fail));
+}
+
+// From M (strict lower, in m) and the pivots d (in dv): the tile's
+// L = M diag(d)^{1/2} into `tile` (upper part and zero_right columns set
+// to zero) and L^{-1} = diag(d)^{-1/2} M^{-1} into `tinv`.  M^{-1}: its
+// 8 x 8 diagonal blocks by substitution (one column per thread), then
+// recursive doubling.  z and u are scratch.
+template <typename T>
+__device__ void tile_outputs_from_m(T (*m)[kTile + 1], const T* dv, T (*z)[kTile + 1], T (*u)[kTile + 1], T* rs,
+                                    T* tile, int64_t ld, int nb, int zero_right, T* tinv) {
+    const int tid = threadIdx.x;
+    for (int e = tid; e < kTile * kTile; e += kTileThreads) z[e / kTile][e % kTile] = T(0);
+    if (tid < kTile) rs[tid] = rsq<T>(dv[tid]);
+    __syncthreads();
+    if (tid < kTile) {  // column c of the inverse of c's 8-block
+        const int c = tid, b0 = c & ~7;
+        z[c][c] = T(1);
+        for (int i = c + 1; i < b0 + 8; ++i) {
+            T acc = m[i][c];
+            for (int k = c + 1; k < i; ++k) acc = fma(m[i][k], z[k][c], acc);
+            z[i][c] = -acc;
+        }
+    }
+    __syncthreads();
+    unit_inverse_doubling<T>(m, z, u);
+    for (int e = tid; e < kTile * kTile; e += kTileThreads) {
+        const int r = e / kTile, c = e % kTile;
+        if (r >= nb || c >= nb) continue;
+        T lv = T(0), xv = T(0);
+        if (c < r) {
+            lv = m[r][c] * (dv[c] * rs[c]);
+            xv = z[r][c] * rs[r];
+        } else if (c == r) {
+            lv = dv[r] * rs[r];
+            xv = rs[r];
+        }
+        tile[(int64_t)r * ld + c] = lv;
+        tinv[r * kTile + c] = xv;
+    }
+    for (int e = tid; e < nb * zero_right; e += kTileThreads) {
+        const int r = e / zero_right, c = e % zero_right;
+        tile[(int64_t)r * ld + nb + c] = T(0);
+    }
+    __syncthreads();
+}
 
 }  // namespace sgb
