@@ -53,6 +53,7 @@ namespace {
 constexpr int TC_BM = 128;
 constexpr int TC_BK = 32;
 constexpr int kMaxTcProbs = 4;
+constexpr int64_t kTcSmCount = 148;  // CTAs one launch should keep busy (152 SMs)
 constexpr int kMaxSplitJobs = 2 * kMaxTcProbs;  // probs x operands
 constexpr long long kSpinLimit = 1ll << 22;         // bounded mbarrier waits (~1 s)
 
@@ -224,6 +225,7 @@ struct TcProb {
 struct TcLaunch {
     TcProb p[kMaxTcProbs];
     int32_t np;
+    int32_t ks;    // CTAs per output tile (a cluster), each over a K slice
     int32_t* err;  // set to SGB_ERR_TIMEOUT if a bounded wait gave up
 };
 
@@ -335,6 +337,25 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
         : "memory");
 }
 
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// FP32 load from the shared memory of CTA `rank` of this cluster.
+__device__ __forceinline__ float ld_dsmem(uint32_t local_addr, uint32_t rank) {
+    uint32_t raddr;
+    float v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(raddr) : "r"(local_addr), "r"(rank));
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(raddr) : "memory");
+    return v;
+}
+
 template <int S, int BN>
 struct TcSmem {
     static constexpr int kA = S * TC_BM * TC_BK * 2;   // bytes of A slices per stage
@@ -342,7 +363,16 @@ struct TcSmem {
     static constexpr int kStage = kA + kB;
     static constexpr int kBudget = 225 * 1024;
     static constexpr int kStages = (kBudget / kStage) > 4 ? 4 : (kBudget / kStage);
-    static constexpr int kBytes = kStages * kStage + 1024 + 256;
+    static constexpr int kNacc = S < 6 ? S : 6;
+    // the epilogue stages the FP64 tile (row stride BN + 1) in the idle
+    // stage memory; a K-split CTA keeps its FP32 level accumulators there
+    // too and stages only its (at most half of the) rows
+    static constexpr int kOut = TC_BM * (BN + 1) * 8;
+    static constexpr int kRed = kNacc * TC_BM * BN * 4 + (TC_BM / 2) * (BN + 1) * 8;
+    static_assert(kOut <= kStages * kStage, "staging fits the stage memory");
+    static constexpr int kData = kStages * kStage > kRed ? kStages * kStage : kRed;
+    static constexpr int kBytes = kData + 1024 + 256;
+    static_assert(kBytes <= 227 * 1024, "shared memory per CTA");
     static_assert(kStages >= 2, "at least two pipeline stages");
 };
 
@@ -356,13 +386,15 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     using SM = TcSmem<S, BN>;
     constexpr int NS = SM::kStages;
-    uint64_t* full = (uint64_t*)(smem + NS * SM::kStage);
+    uint64_t* full = (uint64_t*)(smem + SM::kData);
     uint64_t* empty = full + NS;
     uint64_t* done = empty + NS;
     uint32_t* tmem_slot = (uint32_t*)(done + 1);
     int* flags = (int*)(tmem_slot + 1);  // [0] error seen
 
-    const int tile = blockIdx.x;
+    const int ks = L.ks;  // CTAs of this tile's cluster, one K slice each
+    const uint32_t rank = ks > 1 ? cluster_rank() : 0u;
+    const int tile = blockIdx.x / ks;
     int pi = 0;
 #pragma unroll 1
     for (int q = 1; q < L.np; ++q)
@@ -402,13 +434,16 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    const int nkb = P.Kpad / TC_BK;
+    const int nkb_all = P.Kpad / TC_BK;
+    const int kb0 = (int)((int64_t)rank * nkb_all / ks), kb1 = (int)((int64_t)(rank + 1) * nkb_all / ks);
+    const int nkb = kb1 - kb0;  // this CTA's K slice
     const uint32_t sbase = smem_u32(smem);
     // chunk bases: A chunk (p, mt, kb) and B chunk (q, ntile, kb)
     const unsigned char* Ag = (const unsigned char*)(P.A + (int64_t)inst * P.strideA);
     const unsigned char* Bg = (const unsigned char*)(P.B + (int64_t)inst * P.strideB);
     const int64_t a_slice = (int64_t)P.Mpad * P.Kpad * 2, b_slice = (int64_t)P.Npad * P.Kpad * 2;
-    const int64_t a_tile = (int64_t)mt * nkb * (TC_BM * TC_BK * 2), b_tile = (int64_t)ntile * nkb * (BN * TC_BK * 2);
+    const int64_t a_tile = ((int64_t)mt * nkb_all + kb0) * (TC_BM * TC_BK * 2);
+    const int64_t b_tile = ((int64_t)ntile * nkb_all + kb0) * (BN * TC_BK * 2);
 
     if (warp == 4) {
         // producer
@@ -466,71 +501,145 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         }
     }
 
-    // epilogue warps 0-3
+    // epilogue: the level sums of every element become one FP64 value
+    // (exact two-sum of the FP32 accumulators, integer widening, one FP64
+    // add, power-of-two scale), staged row-major in shared memory, then
+    // written out -- alpha, beta and C_in applied -- with consecutive
+    // threads on consecutive columns, so global loads and stores coalesce.
     bool ok = true;
     if (warp < 4) {
         if (!mbar_wait(smem_u32(done), 0)) ok = false;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
     const bool all_ok = !__syncthreads_or(!ok || flags[0] != 0);
-
-    if (all_ok && warp < 4) {
-        const int m = m0 + warp * 32 + lane;
-        const int64_t mrow = m;
-        const int eAm = (m < P.M) ? P.eA[(int64_t)inst * P.strideEA + m] : 0;
-        double* C = P.Cout + (int64_t)inst * P.strideC;
-        const double* Ci = P.Cin ? P.Cin + (int64_t)inst * P.strideCin : nullptr;
-        const int32_t* eB = P.eB + (int64_t)inst * P.strideEB;
-        const bool neg = P.alpha == -1.0, unit = P.alpha == 1.0 || neg;
-#pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-            float v[NACC][16];
-            const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + c0;
-            if (nkb > 0) {
+    if (!all_ok && tid == 0 && L.err != nullptr) atomicExch(L.err, SGB_ERR_TIMEOUT);
+    double* C = P.Cout + (int64_t)inst * P.strideC;
+    const double* Ci = P.Cin ? P.Cin + (int64_t)inst * P.strideCin : nullptr;
+    const int32_t* eA = P.eA + (int64_t)inst * P.strideEA;
+    const int32_t* eB = P.eB + (int64_t)inst * P.strideEB;
+    auto combine = [&](const float (&vv)[NACC], int eAm, int eBn) -> double {
+        if (eAm == 0 || eBn == 0) return 0.0;
+        float hi = vv[0], lo = 0.f;
 #pragma unroll
-                for (int l = 0; l < NACC; ++l) tmem_ld16(ta + l * BN, v[l]);
-            } else {
+        for (int l = 1; l < NACC; ++l) {
+            const float s2 = hi + vv[l];
+            const float bb = s2 - hi;
+            lo += (hi - (s2 - bb)) + (vv[l] - bb);
+            hi = s2;
+        }
+        const float h2 = hi + lo;
+        lo = lo - (h2 - hi);
+        hi = h2;
+        return scale_pow2(f32_to_f64(hi) + f32_to_f64(lo), eAm + eBn - 2058);
+    };
+    // rows [r_lo, r_hi) of the tile are staged in Ds[row - r_lo][col] and written by this CTA
+    int r_lo = 0, r_hi = TC_BM;
+    double* Ds;
+    if (ks > 1) {
+        // K split over the cluster: each CTA parks its level accumulators in
+        // its (now idle) stage memory as R[l][col][row]; after a cluster
+        // barrier CTA q sums rows [q*128/ks, (q+1)*128/ks) over all CTAs
+        // through distributed shared memory -- exact, the level sums being
+        // integers below 2^24 units over the whole K.
+        float* R = (float*)smem;
+        Ds = (double*)(smem + NACC * TC_BM * BN * 4);
+        if (all_ok && warp < 4) {
+            const int row = warp * 32 + lane;
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                float v[NACC][16];
+                const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + c0;
+                if (nkb > 0) {
+#pragma unroll
+                    for (int l = 0; l < NACC; ++l) tmem_ld16(ta + l * BN, v[l]);
+                } else {
+#pragma unroll
+                    for (int l = 0; l < NACC; ++l)
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) v[l][i] = 0.f;
+                }
 #pragma unroll
                 for (int l = 0; l < NACC; ++l)
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) v[l][i] = 0.f;
+                    for (int i = 0; i < 16; ++i) R[(l * BN + c0 + i) * TC_BM + row] = v[l][i];
             }
-            if (m < P.M) {
+        }
+        cluster_sync_all();
+        r_lo = (int)(rank * TC_BM / ks);
+        r_hi = (int)((rank + 1) * TC_BM / ks);
+        const int nr = r_hi - r_lo;
+        const uint32_t Rs = smem_u32(R);
+#pragma unroll 1
+        for (int e = tid; e < nr * BN; e += TC_THREADS2) {
+            const int row = r_lo + e % nr, col = e / nr;
+            float acc[NACC][8];
+#pragma unroll
+            for (int l = 0; l < NACC; ++l)
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    acc[l][q] = q < ks ? ld_dsmem(Rs + (uint32_t)(((l * BN + col) * TC_BM + row) * 4), (uint32_t)q)
+                                       : 0.f;
+            float vv[NACC];
+#pragma unroll
+            for (int l = 0; l < NACC; ++l) {
+                float t = 0.f;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) t += acc[l][q];
+                vv[l] = t;
+            }
+            const int m = m0 + row, n = n0 + col;
+            Ds[(row - r_lo) * (BN + 1) + col] =
+                combine(vv, m < P.M ? eA[m] : 0, n < P.N ? eB[n] : 0);
+        }
+    } else {
+        Ds = (double*)smem;
+        if (all_ok && warp < 4) {
+            const int row = warp * 32 + lane, m = m0 + row;
+            const int eAm = m < P.M ? eA[m] : 0;
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                float v[NACC][16];
+                const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + c0;
+                if (nkb > 0) {
+#pragma unroll
+                    for (int l = 0; l < NACC; ++l) tmem_ld16(ta + l * BN, v[l]);
+                } else {
+#pragma unroll
+                    for (int l = 0; l < NACC; ++l)
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) v[l][i] = 0.f;
+                }
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
                     const int n = n0 + c0 + i;
-                    if (n >= P.N) break;
-                    if (P.lower_only && n > m) continue;
-                    double r = 0.0;
-                    const int eBn = eB[n];
-                    if (eAm != 0 && eBn != 0) {
-                        float hi = v[0][i], lo = 0.f;
+                    float vv[NACC];
 #pragma unroll
-                        for (int l = 1; l < NACC; ++l) {
-                            const float s2 = hi + v[l][i];
-                            const float bb = s2 - hi;
-                            lo += (hi - (s2 - bb)) + (v[l][i] - bb);
-                            hi = s2;
-                        }
-                        const float h2 = hi + lo;
-                        lo = lo - (h2 - hi);
-                        hi = h2;
-                        r = f32_to_f64(hi) + f32_to_f64(lo);
-                        r = scale_pow2(r, eAm + eBn - 2058);
-                    }
-                    if (!unit) r *= P.alpha;
-                    else if (neg) r = -r;
-                    if (Ci != nullptr && P.beta != 0.0) {
-                        const double cv = P.transCin ? Ci[(int64_t)n * P.ldcin + mrow] : Ci[mrow * P.ldcin + n];
-                        r = fma(P.beta, cv, r);
-                    }
-                    C[mrow * P.ldc + n] = r;
+                    for (int l = 0; l < NACC; ++l) vv[l] = v[l][i];
+                    Ds[row * (BN + 1) + c0 + i] = combine(vv, eAm, n < P.N ? eB[n] : 0);
                 }
             }
         }
-    } else if (!all_ok && tid == 0 && L.err != nullptr) {
-        atomicExch(L.err, SGB_ERR_TIMEOUT);
     }
+    __syncthreads();
+    if (all_ok) {
+        const int nr = r_hi - r_lo;
+        const bool neg = P.alpha == -1.0, unit = P.alpha == 1.0 || neg;
+#pragma unroll 1
+        for (int e = tid; e < nr * BN; e += TC_THREADS2) {
+            const int row = r_lo + e / BN, col = e % BN;
+            const int m = m0 + row, n = n0 + col;
+            if (m >= P.M || n >= P.N || (P.lower_only && n > m)) continue;
+            double r = Ds[(row - r_lo) * (BN + 1) + col];
+            if (!unit) r *= P.alpha;
+            else if (neg) r = -r;
+            if (Ci != nullptr && P.beta != 0.0) {
+                const double cv = P.transCin ? Ci[(int64_t)n * P.ldcin + m] : Ci[(int64_t)m * P.ldcin + n];
+                r = fma(P.beta, cv, r);
+            }
+            C[(int64_t)m * P.ldc + n] = r;
+        }
+    }
+    if (ks > 1) cluster_sync_all();  // peers may still read this CTA's accumulators
     if (!all_ok && tid == 0) {
         // drain (bounded): the final commit, then any stage still being filled
         mbar_wait(smem_u32(done), 0);
@@ -555,8 +664,25 @@ cudaError_t set_smem_attr() {
 
 template <int S, int BN>
 cudaError_t launch_tc(TcLaunch& L, int total_tiles, cudaStream_t s) {
-    k_gemm_tc<S, BN><<<total_tiles, TC_THREADS2, TcSmem<S, BN>::kBytes, s>>>(L);
-    return cudaGetLastError();
+    if (L.ks <= 1) {
+        k_gemm_tc<S, BN><<<total_tiles, TC_THREADS2, TcSmem<S, BN>::kBytes, s>>>(L);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3((unsigned)(total_tiles * L.ks));
+    cfg.blockDim = dim3(TC_THREADS2);
+    cfg.dynamicSmemBytes = TcSmem<S, BN>::kBytes;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    memset(at, 0, sizeof(at));
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)L.ks;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_gemm_tc<S, BN>, L);
 }
 
 std::mutex g_attr_mu;
@@ -611,12 +737,26 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
     char* base = (char*)ws;
     size_t off = 0;
     int64_t split_ctas = 0, gemm_tiles = 0;
-    // 128 x 64 tiles unless that leaves most SMs idle; then 128 x 32.
-    int64_t tiles64 = 0;
+    // 128 x 64 tiles.  When they leave most SMs idle, each tile's K range is
+    // split over a cluster of ks CTAs (exact FP32 reduction through
+    // distributed shared memory); failing that, 128 x 32 tiles.
+    int64_t tiles64 = 0, minkb = 1 << 30;
     for (int i = 0; i < np; ++i)
-        if (probs[i].M > 0 && probs[i].N > 0 && probs[i].batch > 0)
+        if (probs[i].M > 0 && probs[i].N > 0 && probs[i].batch > 0) {
             tiles64 += ceil_div(probs[i].M, TC_BM) * ceil_div(probs[i].N, kTcBN) * probs[i].batch;
-    const int bn = tiles64 < 148 ? 32 : 64;
+            int64_t kp = 0;
+            for (int t = 0; t < probs[i].nterms; ++t) kp += ceil_div(probs[i].term[t].K, TC_BK);
+            minkb = kp < minkb ? kp : minkb;
+        }
+    int ks = 1;
+    if (tiles64 > 0 && tiles64 < 100) {
+        int64_t k = kTcSmCount / tiles64;
+        if (k > 8) k = 8;
+        if (k > minkb) k = minkb;
+        ks = k < 1 ? 1 : (int)k;
+    }
+    const int bn = (ks > 1 || tiles64 >= 148) ? 64 : 32;
+    TL.ks = ks;
     for (int i = 0; i < np; ++i) {
         const GemmProb<double>& p = probs[i];
         if (p.M <= 0 || p.N <= 0 || p.batch <= 0) continue;
