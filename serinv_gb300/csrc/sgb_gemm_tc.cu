@@ -81,6 +81,7 @@ struct SplitJob {
 };
 
 constexpr int kSplitRows = 8;
+constexpr int kSplitThreads = 512;  // four warps per scheduler: the split is latency bound
 constexpr int kSplitLd = kTcMaxK + 1;  // odd stride: conflict-free row and column access
 
 struct SplitLaunch {
@@ -114,8 +115,7 @@ __device__ __forceinline__ void digits(double x, int Erow, int (&d)[S]) {
     if (bits >> 63) X = -X;
 #pragma unroll
     for (int p = S - 1; p >= 1; --p) {
-        int v = (int)(X & 127);
-        if (v >= 64) v -= 128;
+        const int v = ((int)(X & 127) ^ 64) - 64;  // balanced digit in [-64, 63]
         d[p] = v;
         X = (X - v) >> 7;
     }
@@ -129,7 +129,7 @@ __device__ __forceinline__ void digits(double x, int Erow, int (&d)[S]) {
 // read -- padding rows and the K padding of each term as zeros, so the
 // buffers need no clearing beforehand.
 template <int S>
-__global__ void __launch_bounds__(256) k_split(const __grid_constant__ SplitLaunch L) {
+__global__ void __launch_bounds__(kSplitThreads) k_split(const __grid_constant__ SplitLaunch L) {
     __shared__ double t[kSplitRows][kSplitLd];
     __shared__ int ex[kSplitRows];
     const SplitJob& J = L.j[find_job(L, blockIdx.x)];
@@ -137,40 +137,45 @@ __global__ void __launch_bounds__(256) k_split(const __grid_constant__ SplitLaun
     const int inst = local / J.strips;
     const int r0 = (local - inst * J.strips) * kSplitRows;
     const int tid = threadIdx.x;
-    for (int e = tid; e < kSplitRows * J.Kpad; e += 256) t[e / J.Kpad][e % J.Kpad] = 0.0;
-    __syncthreads();
-    // Loads are issued kSplitBatch at a time per thread before any is
-    // stored, so a CTA has its whole strip in flight at once.
-    constexpr int kSplitBatch = 6;
+    // Each source covers [koff, koff + Kp) of the strip (Kp = K rounded up to
+    // 32); elements past K or past the last row are written as zeros, so
+    // every element of the strip is written once.  A thread issues all its
+    // loads (at most kSplitPer) before it stores any, so a CTA keeps its
+    // whole strip in flight at once.
+    constexpr int kSplitPer = kSplitRows * kTcMaxK / kSplitThreads;
     for (int q = 0; q < J.nsrc; ++q) {
         const SplitSrc& src = J.src[q];
         const double* X = src.X + (int64_t)inst * src.stride;
-        const int total = kSplitRows * src.K;
+        const int Kp = (src.K + TC_BK - 1) / TC_BK * TC_BK;
+        const int total = kSplitRows * Kp;
         const bool rowmajor = src.ld_k == 1;  // else columns contiguous in r
-        for (int e0 = tid; e0 < total; e0 += 256 * kSplitBatch) {
-            double v[kSplitBatch];
-            int dst[kSplitBatch];
+        for (int e0 = tid; e0 < total; e0 += kSplitThreads * kSplitPer) {
+            double v[kSplitPer];
+            int dst[kSplitPer];
 #pragma unroll
-            for (int u = 0; u < kSplitBatch; ++u) {
-                const int e = e0 + u * 256;
+            for (int u = 0; u < kSplitPer; ++u) {
+                const int e = e0 + u * kSplitThreads;
                 int rr, k;
                 if (rowmajor) {  // a warp reads 32 consecutive k of one row
-                    rr = e / src.K;
-                    k = e - rr * src.K;
+                    rr = e / Kp;
+                    k = e - rr * Kp;
                 } else {  // eight rows of four k per warp
                     k = e / kSplitRows;
                     rr = e % kSplitRows;
                 }
                 const int r = r0 + rr;
-                const bool in = e < total && r < J.R;
+                const bool in = e < total;
+                const bool load = in && r < J.R && k < src.K;
                 dst[u] = in ? rr * kSplitLd + src.koff + k : -1;
-                v[u] = in ? __ldg(X + (int64_t)r * src.ld_r + (int64_t)k * src.ld_k) : 0.0;
+                v[u] = load ? __ldg(X + (int64_t)r * src.ld_r + (int64_t)k * src.ld_k) : 0.0;
             }
 #pragma unroll
-            for (int u = 0; u < kSplitBatch; ++u)
+            for (int u = 0; u < kSplitPer; ++u)
                 if (dst[u] >= 0) (&t[0][0])[dst[u]] = v[u];
         }
     }
+    if (J.nsrc == 0)
+        for (int e = tid; e < kSplitRows * J.Kpad; e += kSplitThreads) t[e / J.Kpad][e % J.Kpad] = 0.0;
     __syncthreads();
     const int warp = tid >> 5, lane = tid & 31;
     if (warp < kSplitRows) {
@@ -189,18 +194,33 @@ __global__ void __launch_bounds__(256) k_split(const __grid_constant__ SplitLaun
     __nv_bfloat16* out = J.out + (int64_t)inst * J.out_stride;
     const int64_t slice = (int64_t)J.Rpad * J.Kpad;
     const int nkb = J.Kpad / 32, RT = J.RT;
-    for (int e = tid; e < kSplitRows * J.Kpad; e += 256) {
-        const int rr = e % kSplitRows, k = e / kSplitRows;
+    // Eight consecutive k of one row are contiguous (16 bytes) in the core-
+    // matrix order [k/8][row/8][row%8][k%8] of a chunk: a thread digits one
+    // such group and writes each slice with a single 16-byte store.
+    const float w7[7] = {1.0f, 0x1p-7f, 0x1p-14f, 0x1p-21f, 0x1p-28f, 0x1p-35f, 0x1p-42f};
+    for (int g = tid; g < kSplitRows * (J.Kpad / 8); g += kSplitThreads) {
+        const int rr = g % kSplitRows, k0 = (g / kSplitRows) * 8;
         const int r = r0 + rr;
-        int d[S];
-        digits<S>(t[rr][k], ex[rr], d);
-        // chunk (r / RT, k / 32) of RT x 32 elements in core-matrix order:
-        // [k/8][row/8][row%8][k%8]
-        const int rt = r / RT, ri = r % RT, kb = k >> 5, kk = k & 31;
+        const int rt = r / RT, ri = r % RT, kb = k0 >> 5, kk = k0 & 31;
         const int64_t o = ((int64_t)rt * nkb + kb) * (RT * 32) + ((kk >> 3) * (RT >> 3) + (ri >> 3)) * 64 +
-                          (ri & 7) * 8 + (kk & 7);
+                          (ri & 7) * 8;
+        uint32_t packed[S][4];
 #pragma unroll
-        for (int p = 0; p < S; ++p) out[p * slice + o] = __float2bfloat16_rn(ldexpf((float)d[p], -7 * p));
+        for (int j = 0; j < 8; j += 2) {
+            int d0[S], d1[S];
+            digits<S>(t[rr][k0 + j], ex[rr], d0);
+            digits<S>(t[rr][k0 + j + 1], ex[rr], d1);
+#pragma unroll
+            for (int p = 0; p < S; ++p) {
+                // w_p = d * 2^(-7p) is exact in bf16 (|d| <= 128)
+                const __nv_bfloat162 v = __floats2bfloat162_rn((float)d0[p] * w7[p], (float)d1[p] * w7[p]);
+                packed[p][j >> 1] = *reinterpret_cast<const uint32_t*>(&v);
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < S; ++p)
+            *reinterpret_cast<uint4*>(out + p * slice + o) =
+                make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
     }
 }
 
@@ -347,11 +367,15 @@ __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-// FP32 load from the shared memory of CTA `rank` of this cluster.
-__device__ __forceinline__ float ld_dsmem(uint32_t local_addr, uint32_t rank) {
+// Address of `local_addr` in the shared memory of CTA `rank` of this cluster.
+__device__ __forceinline__ uint32_t dsmem_addr(uint32_t local_addr, uint32_t rank) {
     uint32_t raddr;
-    float v;
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(raddr) : "r"(local_addr), "r"(rank));
+    return raddr;
+}
+
+__device__ __forceinline__ float ld_dsmem(uint32_t raddr) {
+    float v;
     asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(raddr) : "memory");
     return v;
 }
@@ -371,7 +395,8 @@ struct TcSmem {
     static constexpr int kRed = kNacc * TC_BM * BN * 4 + (TC_BM / 2) * (BN + 1) * 8;
     static_assert(kOut <= kStages * kStage, "staging fits the stage memory");
     static constexpr int kData = kStages * kStage > kRed ? kStages * kStage : kRed;
-    static constexpr int kBytes = kData + 1024 + 256;
+    static constexpr int kExOff = kData + 256;  // staged row / column exponents
+    static constexpr int kBytes = kData + 1024 + 1024;
     static_assert(kBytes <= 227 * 1024, "shared memory per CTA");
     static_assert(kStages >= 2, "at least two pipeline stages");
 };
@@ -515,8 +540,16 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
     if (!all_ok && tid == 0 && L.err != nullptr) atomicExch(L.err, SGB_ERR_TIMEOUT);
     double* C = P.Cout + (int64_t)inst * P.strideC;
     const double* Ci = P.Cin ? P.Cin + (int64_t)inst * P.strideCin : nullptr;
-    const int32_t* eA = P.eA + (int64_t)inst * P.strideEA;
-    const int32_t* eB = P.eB + (int64_t)inst * P.strideEB;
+    // the tile's row and column exponents, staged once
+    int* eAs = (int*)(smem + SM::kExOff);
+    int* eBs = eAs + TC_BM;
+    {
+        const int32_t* eA = P.eA + (int64_t)inst * P.strideEA;
+        const int32_t* eB = P.eB + (int64_t)inst * P.strideEB;
+        if (tid < TC_BM) eAs[tid] = (m0 + tid < P.M) ? eA[m0 + tid] : 0;
+        else if (tid - TC_BM < BN) eBs[tid - TC_BM] = (n0 + tid - TC_BM < P.N) ? eB[n0 + tid - TC_BM] : 0;
+    }
+    __syncthreads();
     auto combine = [&](const float (&vv)[NACC], int eAm, int eBn) -> double {
         if (eAm == 0 || eBn == 0) return 0.0;
         float hi = vv[0], lo = 0.f;
@@ -568,7 +601,9 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         r_lo = (int)(rank * TC_BM / ks);
         r_hi = (int)((rank + 1) * TC_BM / ks);
         const int nr = r_hi - r_lo;
-        const uint32_t Rs = smem_u32(R);
+        uint32_t rb[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) rb[q] = q < ks ? dsmem_addr(smem_u32(R), (uint32_t)q) : 0u;
 #pragma unroll 1
         for (int e = tid; e < nr * BN; e += TC_THREADS2) {
             const int row = r_lo + e % nr, col = e / nr;
@@ -577,8 +612,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
             for (int l = 0; l < NACC; ++l)
 #pragma unroll
                 for (int q = 0; q < 8; ++q)
-                    acc[l][q] = q < ks ? ld_dsmem(Rs + (uint32_t)(((l * BN + col) * TC_BM + row) * 4), (uint32_t)q)
-                                       : 0.f;
+                    acc[l][q] = q < ks ? ld_dsmem(rb[q] + (uint32_t)(((l * BN + col) * TC_BM + row) * 4)) : 0.f;
             float vv[NACC];
 #pragma unroll
             for (int l = 0; l < NACC; ++l) {
@@ -587,15 +621,13 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
                 for (int q = 0; q < 8; ++q) t += acc[l][q];
                 vv[l] = t;
             }
-            const int m = m0 + row, n = n0 + col;
-            Ds[(row - r_lo) * (BN + 1) + col] =
-                combine(vv, m < P.M ? eA[m] : 0, n < P.N ? eB[n] : 0);
+            Ds[(row - r_lo) * (BN + 1) + col] = combine(vv, eAs[row], eBs[col]);
         }
     } else {
         Ds = (double*)smem;
         if (all_ok && warp < 4) {
-            const int row = warp * 32 + lane, m = m0 + row;
-            const int eAm = m < P.M ? eA[m] : 0;
+            const int row = warp * 32 + lane;
+            const int eAm = eAs[row];
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 float v[NACC][16];
@@ -611,11 +643,10 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
                 }
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
-                    const int n = n0 + c0 + i;
                     float vv[NACC];
 #pragma unroll
                     for (int l = 0; l < NACC; ++l) vv[l] = v[l][i];
-                    Ds[row * (BN + 1) + c0 + i] = combine(vv, eAm, n < P.N ? eB[n] : 0);
+                    Ds[row * (BN + 1) + c0 + i] = combine(vv, eAm, eBs[c0 + i]);
                 }
             }
         }
@@ -860,11 +891,11 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
     if (split_ctas > 0) {
         prof_before(s);
         switch (S) {
-            case 3: k_split<3><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
-            case 4: k_split<4><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
-            case 5: k_split<5><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
-            case 6: k_split<6><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
-            default: k_split<7><<<(unsigned)split_ctas, 256, 0, s>>>(SL); break;
+            case 3: k_split<3><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
+            case 4: k_split<4><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
+            case 5: k_split<5><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
+            case 6: k_split<6><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
+            default: k_split<7><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
         }
         prof_after(SGB_KCLASS_SPLIT, s, 0.0);
         cudaError_t e = cudaGetLastError();

@@ -9,31 +9,33 @@
 // FP64 pipe allows.  Roles (G CTAs, one per SM):
 //
 //   CTA 0        factorizer: diagonal tile p as L = M D^{1/2} (the pivot
-//                pipeline of factor_tile_m), publishes M and the pivots d
-//                (counter F), then waits for the helpers (counter H2)
-//                before tile p+1;
-//   CTAs 1..kNH  helpers: once M_p is out, the rows of tile-row p+1 in
-//                column block p by unit-triangular substitution
-//                (Y M^T = B, X = Y D^{-1/2}; counter H1), then their rows
-//                of the update of tile (p+1, p+1) (counter H2); after
+//                pipeline of factor_tile_m), whose warp 4 publishes the
+//                columns of M and the pivots d as they are produced
+//                (counter of published columns), then counter F at the end
+//                of the tile; waits for the helpers (counter H2) before
+//                tile p+1;
+//   CTAs 1..kNH  helpers: the rows of tile-row p+1 in column block p by
+//                unit-triangular substitution (Y M^T = B, X = Y D^{-1/2}),
+//                following the published columns (counter H1), then their
+//                rows of the update of tile (p+1, p+1) (counter H2); after
 //                barrier B they apply column block p to their rows of
 //                tile-row p+2 (tiles (p+2, p+1) and (p+2, p+2)), so
 //                nothing the next step needs waits for the bulk update;
-//   CTA kNH+1    inverter: from M_p, d_p the tile's L (into the matrix)
-//                and L^{-1} (for the bulk TRSM; counter I);
-//   CTAs kNH+2.. workers: the other rows below tile p times L_pp^{-T}
-//                (after I), barrier B (with the helpers), the rank-32
-//                update of the rest of the trailing panel, barrier C
-//                (workers only).
+//   CTA kNH+1    L writer: from M_p, d_p the tile's L into the matrix
+//                (counter I);
+//   CTAs kNH+2.. workers: the other rows below tile p, by the same
+//                substitution following the published columns, barrier B
+//                (with the helpers), the rank-32 update of the rest of the
+//                trailing panel (the next tile's operands loaded during the
+//                current tile's FMAs), barrier C (workers only).
 //
-// M/d and L^{-1} alternate between two buffers by the parity of p; the
-// factorizer waits for the inverter before overwriting a buffer.  Every
-// wait is a bounded poll of a word in global memory: one that does not
-// complete within the limit sets the status word to SGB_ERR_TIMEOUT and the
-// CTA leaves (the cooperative launch guarantees that all CTAs are
-// resident, so no wait depends on an unscheduled CTA).  Data produced by
-// other CTAs is read with ld.global.cg (L2), never from a possibly stale
-// L1 line.
+// M and d alternate between two buffers by the parity of p; the factorizer
+// waits for the L writer before overwriting a buffer.  Every wait is a
+// bounded poll of a word in global memory: one that does not complete
+// within the limit sets the status word to SGB_ERR_TIMEOUT and the CTA
+// leaves (the cooperative launch guarantees that all CTAs are resident, so
+// no wait depends on an unscheduled CTA).  Data produced by other CTAs is
+// read with ld.global.cg (L2), never from a possibly stale L1 line.
 #include <math.h>
 
 #include "sgb_internal.cuh"
@@ -47,7 +49,7 @@ constexpr int NT = 256;
 constexpr long long kBarrierSpin = 1ll << 22;
 constexpr int kNH = 8;                 // helper CTAs of the next diagonal tile
 constexpr int kHelpRows = kTile / kNH;  // rows of a tile-row per helper
-constexpr int kInv = kNH + 1;           // the inverter CTA
+constexpr int kInv = kNH + 1;           // the L writer CTA
 constexpr int kW0 = kNH + 2;            // first worker CTA
 
 template <typename T>
@@ -58,10 +60,11 @@ struct PanelArgs {
     int64_t r1rows, r1ld;
     T* r2;
     int64_t r2rows, r2ld;
-    T* scratch;  // [2][32][32] L^{-1}, [2][32][32] M, [2][32] d
+    T* scratch;  // [2][32][32] (unused), [2][32][32] M^T by column, [2][32] d
     int32_t* info;
     int64_t row0;
-    unsigned* bar;    // [0] F, [1] I, [2] H1, [3] H2, [4..5] barrier B, [6..7] barrier C; zero at launch
+    unsigned* bar;    // [0] F, [1] I, [2] H1, [3] H2, [4] barrier B, [6] barrier C,
+                      // [8] columns of M published; zero at launch
     int32_t* status;  // SGB_ERR_TIMEOUT on a stuck wait
 };
 
@@ -80,32 +83,28 @@ __device__ __forceinline__ bool status_bad(const int32_t* status) {
     return ld_acquire((const unsigned*)status) != 0u;
 }
 
-// Barrier over `nblocks` CTAs on the counter/generation pair cg[0], cg[1];
-// returns false (on every thread of the CTA) if it timed out.
-__device__ __forceinline__ bool group_barrier(unsigned* cg, unsigned nblocks, unsigned& epoch, int32_t* status,
+// Barrier over `nblocks` CTAs on a monotonic arrival counter: barrier
+// number e (1, 2, ...) completes when the counter reaches e * nblocks.
+// Arrivals are fire-and-forget reductions, so no CTA waits for an atomic's
+// return.  Returns false (on every thread of the CTA) if it timed out.
+__device__ __forceinline__ bool group_barrier(unsigned* cnt, unsigned nblocks, unsigned& epoch, int32_t* status,
                                               int* sflag) {
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned target = epoch + 1;
+        epoch += 1;
+        const unsigned target = epoch * nblocks;
         int ok = 1;
-        if (atomicAdd(&cg[0], 1u) == nblocks - 1) {
-            atomicExch(&cg[0], 0u);
-            __threadfence();
-            atomicExch(&cg[1], target);
-        } else {
-            long long spins = 0;
-            while ((int)(ld_acquire(&cg[1]) - target) < 0) {
-                if (++spins > kBarrierSpin || status_bad(status)) {
-                    ok = 0;
-                    atomicExch(status, SGB_ERR_TIMEOUT);
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
         __threadfence();
-        epoch = target;
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(cnt) : "memory");
+        long long spins = 0;
+        while ((int)(ld_acquire(cnt) - target) < 0) {
+            if (++spins > kBarrierSpin || status_bad(status)) {
+                ok = 0;
+                atomicExch(status, SGB_ERR_TIMEOUT);
+                break;
+            }
+            __nanosleep(32);
+        }
         *sflag = ok && !status_bad(status);
     }
     __syncthreads();
@@ -150,33 +149,72 @@ __device__ __forceinline__ T* row_ptr(const PanelArgs<T>& a, int64_t c1, int64_t
     return a.r2 + (r - a.r1rows) * a.r2ld;
 }
 
-// rows[ty] (ty < 8) <- rows * tinv^T over the w columns from c0, with tinv
-// in S.x; S.tmp is scratch.  Four accumulators per output.
+// One row per warp: row <- row * L^{-T} over the w columns of the row
+// pointer, with L = M diag(d)^{1/2}: Y M^T = row by substitution (lane =
+// column; one shuffle and one FMA per column), X = Y diag(d)^{-1/2}.  The
+// columns of M (transposed in mt) and the pivots dv are consumed as the
+// factorizer publishes them: column k once *colcount >= col_base + k + 1
+// (bounded wait), all available columns loaded at once.  Returns false on a
+// timeout or an error raised elsewhere.
 template <typename T>
-__device__ __forceinline__ void trsm_rows(Smem<T>& S, T* rp, int w) {
-    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
-    S.tmp[ty][tx] = (rp != nullptr && tx < w) ? ldcg(rp + tx) : T(0);
-    __syncthreads();
-    const int kend = (tx < w - 1 ? tx : w - 1) + 1;
-    T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+__device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T* dv, const unsigned* colcount,
+                                              unsigned col_base, int32_t* status) {
+    const int tx = threadIdx.x & 31;
+    T y = tx < w ? ldcg(rp + tx) : T(0);
     int k = 0;
-    for (; k + 3 < kend; k += 4) {
-        a0 = fma(S.tmp[ty][k], S.x[tx][k], a0);
-        a1 = fma(S.tmp[ty][k + 1], S.x[tx][k + 1], a1);
-        a2 = fma(S.tmp[ty][k + 2], S.x[tx][k + 2], a2);
-        a3 = fma(S.tmp[ty][k + 3], S.x[tx][k + 3], a3);
+    long long spins = 0;
+    while (k < w) {
+        int avail = 0;
+        if (tx == 0) {
+            for (;;) {
+                const unsigned c = ld_acquire(colcount);
+                avail = c > col_base ? (int)(c - col_base) : 0;
+                if (avail > k) break;
+                if (++spins > kBarrierSpin || status_bad(status)) {
+                    atomicExch(status, SGB_ERR_TIMEOUT);
+                    avail = -1;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        avail = __shfl_sync(0xffffffffu, avail, 0);
+        if (avail < 0) return false;
+        if (avail > w) avail = w;
+        while (k < avail) {
+            const int nb = (avail - k) < kTile ? (avail - k) : kTile;
+            T mk[kTile];
+#pragma unroll
+            for (int u = 0; u < kTile; ++u) mk[u] = u < nb ? ldcg(mt + (k + u) * kTile + tx) : T(0);
+#pragma unroll
+            for (int u = 0; u < kTile; ++u) {
+                if (u < nb) {
+                    const T yk = __shfl_sync(0xffffffffu, y, k + u);
+                    if (tx > k + u) y = fma(-yk, mk[u], y);
+                }
+            }
+            k += nb;
+        }
     }
-    for (; k < kend; ++k) a0 = fma(S.tmp[ty][k], S.x[tx][k], a0);
-    if (rp != nullptr && tx < w) rp[tx] = (a0 + a1) + (a2 + a3);
-    __syncthreads();
+    if (tx < w) rp[tx] = y * rsq<T>(ldcg(dv + tx));
+    return true;
 }
 
-// dst[32 x 32] <- rows x cols block of a row-major source (zero padded).
+// dst[32 x 32] <- rows x cols block of a row-major source (zero padded);
+// each thread issues its four loads before storing any.
 template <typename T>
 __device__ __forceinline__ void load_block(T (*dst)[kTile + 1], const T* src, int64_t ld, int rows, int cols) {
-    for (int e = threadIdx.x; e < kTile * kTile; e += NT) {
-        const int r = e / kTile, c = e % kTile;
-        dst[r][c] = (r < rows && c < cols) ? ldcg(src + (int64_t)r * ld + c) : T(0);
+    constexpr int U = kTile * kTile / NT;
+    T v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int e = threadIdx.x + u * NT, r = e / kTile, c = e % kTile;
+        v[u] = (r < rows && c < cols) ? ldcg(src + (int64_t)r * ld + c) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int e = threadIdx.x + u * NT;
+        dst[e / kTile][e % kTile] = v[u];
     }
 }
 
@@ -210,9 +248,9 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
     unsigned* H2 = a.bar + 3;
     unsigned* barB = a.bar + 4;
     unsigned* barC = a.bar + 6;
-    T* tinvg = a.scratch;                    // [2][32*32]
-    T* Mg = a.scratch + 2 * kTile * kTile;   // [2][32*32]
-    T* dg = a.scratch + 4 * kTile * kTile;   // [2][32]
+    unsigned* CC = a.bar + 8;
+    T* Mg = a.scratch + 2 * kTile * kTile;  // [2][32*32], column k of M at [k][0..31]
+    T* dg = a.scratch + 4 * kTile * kTile;  // [2][32]
     auto tile_w = [&](int64_t p) -> int { return (int)((m - p * kTile) < kTile ? (m - p * kTile) : kTile); };
 
     if (cta == 0) {
@@ -222,26 +260,25 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
             const int w = tile_w(p);
             if (p >= 1 && !wait_count(H2, (unsigned)(kNH * p), a.status, &S.flag)) return;
             if (p >= 2 && !wait_count(I, (unsigned)(p - 1), a.status, &S.flag)) return;
-            factor_tile_m<T>(S, a.diag + c0 * a.ldd + c0, a.ldd, w, a.info, a.row0 + c0);
-            T* Mo = Mg + (p & 1) * kTile * kTile;
-            T* dout = dg + (p & 1) * kTile;
-            for (int e = tid; e < kTile * kTile; e += NT) Mo[e] = S.x[e / kTile][e % kTile];
-            if (tid < kTile) dout[tid] = S.yv[tid];
+            factor_tile_m<T>(S, a.diag + c0 * a.ldd + c0, a.ldd, w, a.info, a.row0 + c0, Mg + (p & 1) * kTile * kTile,
+                             dg + (p & 1) * kTile, CC, (unsigned)(p * kTile));
             signal(F);
         }
         return;
     }
     if (cta == (unsigned)kInv) {
-        // ---------------- inverter
+        // ---------------- L writer
         for (int64_t p = 0; p < nt; ++p) {
             const int64_t c0 = p * kTile;
             const int w = tile_w(p);
             if (!wait_count(F, (unsigned)(p + 1), a.status, &S.flag)) return;
-            load_block<T>(S.x, Mg + (p & 1) * kTile * kTile, kTile, kTile, kTile);
+            {
+                const T* mt = Mg + (p & 1) * kTile * kTile;
+                for (int e = tid; e < kTile * kTile; e += NT) S.x[e % kTile][e / kTile] = ldcg(mt + e);
+            }
             if (tid < kTile) S.yv[tid] = ldcg(dg + (p & 1) * kTile + tid);
             __syncthreads();
-            tile_outputs_from_m<T>(S.x, S.yv, S.tmp, S.u, &S.s[0][0], a.diag + c0 * a.ldd + c0, a.ldd, w,
-                                   (int)(m - c0 - w), tinvg + (p & 1) * kTile * kTile);
+            tile_l_from_m<T>(S.x, S.yv, a.diag + c0 * a.ldd + c0, a.ldd, w, (int)(m - c0 - w));
             signal(I);
         }
         return;
@@ -258,25 +295,18 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         const int64_t c2 = c1 + w2;
         const bool has_next2 = c2 < m;
         const int w3 = has_next2 ? tile_w(p + 2) : 0;
+        const T* Mp = Mg + (p & 1) * kTile * kTile;
+        const T* dp = dg + (p & 1) * kTile;
 
         if (helper) {
             if (!has_next) break;
-            // rows of tile-row p+1 in column block p: Y M^T = B, X = Y D^{-1/2}
-            if (!wait_count(F, (unsigned)(p + 1), a.status, &S.flag)) return;
-            load_block<T>(S.x, Mg + (p & 1) * kTile * kTile, kTile, kTile, kTile);
-            if (tid < kTile) S.yv[tid] = rsq<T>(ldcg(dg + (p & 1) * kTile + tid));
-            __syncthreads();
+            // rows of tile-row p+1 in column block p (Y M^T = B, X = Y D^{-1/2}),
+            // column by column as the factorizer publishes M; a timeout sets
+            // the status word, which the wait below sees
             if (ty < kHelpRows) {
                 const int r = h * kHelpRows + ty;
-                if (r < w2) {
-                    T* rp = a.diag + (c1 + r) * a.ldd + c0;
-                    T y = tx < w ? ldcg(rp + tx) : T(0);
-                    for (int k = 0; k < w; ++k) {
-                        const T yk = __shfl_sync(0xffffffffu, y, k);
-                        if (tx > k) y = fma(-yk, S.x[tx][k], y);
-                    }
-                    if (tx < w) rp[tx] = y * S.yv[tx];
-                }
+                if (r < w2)
+                    trsm_row_pipe<T>(a.diag + (c1 + r) * a.ldd + c0, w, Mp, dp, CC, (unsigned)(p * kTile), a.status);
             }
             signal(H1);
             if (!wait_count(H1, (unsigned)(kNH * (p + 1)), a.status, &S.flag)) return;
@@ -313,18 +343,14 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         }
 
         // ---------------- workers
-        if (!wait_count(I, (unsigned)(p + 1), a.status, &S.flag)) return;
-        load_block<T>(S.x, tinvg + (p & 1) * kTile * kTile, kTile, kTile, kTile);
-        __syncthreads();
-        // B(p): the rows below tile p except tile-row p+1 (the helpers')
+        // B(p): the rows below tile p except tile-row p+1 (the helpers'),
+        // one row per warp, following the published columns of M
         const unsigned nwk = G - kW0, wk = cta - kW0;
         const int64_t off0 = w2;
         const int64_t nrows = (m - c1) + a.r1rows + a.r2rows - off0;
-        for (int64_t ch = wk; ch * 8 < nrows; ch += nwk) {
-            const int64_t r = ch * 8 + ty;
-            T* rp = r < nrows ? row_ptr(a, c1, off0 + r) + c0 : nullptr;
-            trsm_rows<T>(S, rp, w);
-        }
+        for (int64_t r = (int64_t)wk * 8 + ty; r < nrows; r += (int64_t)nwk * 8)
+            if (!trsm_row_pipe<T>(row_ptr(a, c1, off0 + r) + c0, w, Mp, dp, CC, (unsigned)(p * kTile), a.status))
+                break;
         if (!has_next) break;
         if (!group_barrier(barB, G - 2, epB, a.status, &S.flag)) return;
 
@@ -335,49 +361,83 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         const int64_t total = tiles_d + (n1 + n2) * ntd;
         const int64_t t0 = tiles_d < 3 ? tiles_d : 3;
         const T* Bpan = a.diag + c1 * a.ldd + c0;
-        for (int64_t t = t0 + wk; t < total; t += nwk) {
-            T* Cbase;
-            const T* Abase;
-            int64_t ldc, rows, cj;
+        // Tile t's operands are staged in one of two shared buffers while
+        // tile t+nwk's are being loaded into registers.
+        struct TileRef {
+            T* C;
+            const T* A;
+            int64_t ldc, rows, cols, cj;
+        };
+        auto tile_ref = [&](int64_t t) {
+            TileRef R;
+            int64_t ti;
             if (t < tiles_d) {  // lower tiles of the trailing D, row-major over the triangle
-                int64_t ti = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+                ti = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
                 while (ti * (ti + 1) / 2 > t) --ti;
                 while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-                cj = t - ti * (ti + 1) / 2;
-                Cbase = a.diag + (c1 + ti * kTile) * a.ldd + c1;
-                Abase = a.diag + (c1 + ti * kTile) * a.ldd + c0;
-                ldc = a.ldd;
-                rows = (m - c1) - ti * kTile;
+                R.cj = t - ti * (ti + 1) / 2;
+                R.C = a.diag + (c1 + ti * kTile) * a.ldd + c1;
+                R.A = a.diag + (c1 + ti * kTile) * a.ldd + c0;
+                R.ldc = a.ldd;
+                R.rows = (m - c1) - ti * kTile;
             } else if (t < tiles_d + n1 * ntd) {
-                const int64_t u = t - tiles_d, ti = u / ntd;
-                cj = u % ntd;
-                Cbase = a.r1 + ti * kTile * a.r1ld + c1;
-                Abase = a.r1 + ti * kTile * a.r1ld + c0;
-                ldc = a.r1ld;
-                rows = a.r1rows - ti * kTile;
+                const int64_t u = t - tiles_d;
+                ti = u / ntd;
+                R.cj = u % ntd;
+                R.C = a.r1 + ti * kTile * a.r1ld + c1;
+                R.A = a.r1 + ti * kTile * a.r1ld + c0;
+                R.ldc = a.r1ld;
+                R.rows = a.r1rows - ti * kTile;
             } else {
-                const int64_t u = t - tiles_d - n1 * ntd, ti = u / ntd;
-                cj = u % ntd;
-                Cbase = a.r2 + ti * kTile * a.r2ld + c1;
-                Abase = a.r2 + ti * kTile * a.r2ld + c0;
-                ldc = a.r2ld;
-                rows = a.r2rows - ti * kTile;
+                const int64_t u = t - tiles_d - n1 * ntd;
+                ti = u / ntd;
+                R.cj = u % ntd;
+                R.C = a.r2 + ti * kTile * a.r2ld + c1;
+                R.A = a.r2 + ti * kTile * a.r2ld + c0;
+                R.ldc = a.r2ld;
+                R.rows = a.r2rows - ti * kTile;
             }
-            if (rows > kTile) rows = kTile;
-            int64_t cols = (m - c1) - cj * kTile;
-            if (cols > kTile) cols = kTile;
-            // stage A (rows x w) and B (cols x w) in shared memory
-            for (int e = tid; e < kTile * kTile; e += NT) {
-                const int r = e / kTile, k = e % kTile;
-                S.s[r][k] = (r < rows && k < w) ? ldcg(Abase + (int64_t)r * ldc + k) : T(0);
-                S.tmp[r][k] = (r < cols && k < w) ? ldcg(Bpan + (cj * kTile + r) * a.ldd + k) : T(0);
+            if (R.rows > kTile) R.rows = kTile;
+            R.cols = (m - c1) - R.cj * kTile;
+            if (R.cols > kTile) R.cols = kTile;
+            return R;
+        };
+        constexpr int U = kTile * kTile / NT;
+        T va[U], vb[U];
+        auto fetch = [&](const TileRef& R) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = tid + u * NT, r = e / kTile, k = e % kTile;
+                va[u] = (r < R.rows && k < w) ? ldcg(R.A + (int64_t)r * R.ldc + k) : T(0);
+                vb[u] = (r < R.cols && k < w) ? ldcg(Bpan + (R.cj * kTile + r) * a.ldd + k) : T(0);
+            }
+        };
+        int64_t t = t0 + wk;
+        TileRef cur;
+        if (t < total) {
+            cur = tile_ref(t);
+            fetch(cur);
+        }
+        for (int buf = 0; t < total; t += nwk, buf ^= 1) {
+            T (*As)[kTile + 1] = buf ? S.x : S.s;
+            T (*Bs)[kTile + 1] = buf ? S.u : S.tmp;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = tid + u * NT;
+                As[e / kTile][e % kTile] = va[u];
+                Bs[e / kTile][e % kTile] = vb[u];
             }
             __syncthreads();
+            const TileRef now = cur;
+            if (t + nwk < total) {  // next tile's operands in flight during this tile's FMAs
+                cur = tile_ref(t + nwk);
+                fetch(cur);
+            }
             const int cx = tid & 15, cy = tid >> 4;
             T acc[2][2] = {{T(0), T(0)}, {T(0), T(0)}};
             for (int k = 0; k < w; ++k) {
-                const T a0 = S.s[cy][k], a1 = S.s[cy + 16][k];
-                const T b0 = S.tmp[cx][k], b1 = S.tmp[cx + 16][k];
+                const T a0 = As[cy][k], a1 = As[cy + 16][k];
+                const T b0 = Bs[cx][k], b1 = Bs[cx + 16][k];
                 acc[0][0] = fma(a0, b0, acc[0][0]);
                 acc[0][1] = fma(a0, b1, acc[0][1]);
                 acc[1][0] = fma(a1, b0, acc[1][0]);
@@ -388,12 +448,11 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
 #pragma unroll
                 for (int j2 = 0; j2 < 2; ++j2) {
                     const int r = cy + 16 * i2, c = cx + 16 * j2;
-                    if (r < rows && c < cols) {
-                        T* cp = Cbase + (int64_t)r * ldc + cj * kTile + c;
+                    if (r < now.rows && c < now.cols) {
+                        T* cp = now.C + (int64_t)r * now.ldc + now.cj * kTile + c;
                         *cp = ldcg(cp) - acc[i2][j2];
                     }
                 }
-            __syncthreads();
         }
         if (!group_barrier(barC, G - kW0, epC, a.status, &S.flag)) return;
     }
@@ -437,7 +496,7 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
     a.row0 = info_row0;
     a.bar = bar;
     a.status = status;
-    e = cudaMemsetAsync(bar, 0, 8 * sizeof(unsigned), s);
+    e = cudaMemsetAsync(bar, 0, 16 * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     void* args[] = {(void*)&a};
     prof_before(s);

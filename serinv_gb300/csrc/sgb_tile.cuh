@@ -303,12 +303,20 @@ __device__ void factor_tile(Smem<T>& S, T* tile, int64_t ld, int nb, int zero_ri
 
 // The pipeline part of factor_tile alone: after it, S.x holds the strict
 // lower part of M (zero elsewhere) and S.yv the pivots d (1 beyond nb), so
-// L = M diag(d)^{1/2}.  No inverse, no output: the persistent column-block
-// kernel publishes M and d and leaves the rest to other CTAs.
+// L = M diag(d)^{1/2}.  No inverse, no output.  With `mt` set, warp 4
+// publishes the factor column by column while the pipeline runs: column k
+// of M to mt[k][0..31] (transposed, so a column is one coalesced row) and
+// d_k to dv[k]; every eight columns (every second one from column 24, and
+// after the last) it makes them visible at GPU scope and sets
+// *colcount = col_base + k + 1, so other CTAs can consume the columns as
+// they appear.  Warp 4 takes part in the READY/UPD barriers like a worker
+// either way (it does no FP64 work).
 template <typename T>
-__device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int32_t* info, int64_t row0) {
+__device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int32_t* info, int64_t row0,
+                              T* mt = nullptr, T* dv = nullptr, unsigned* colcount = nullptr,
+                              unsigned col_base = 0) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr int kPipe = 32 + 192;
+    constexpr int kPipe = kTileThreads;  // pivot warp + six worker warps + warp 4
     for (int e = tid; e < kTile * kTile; e += kTileThreads) {
         const int r = e / kTile, c = e % kTile;
         T v = T(0);
@@ -341,7 +349,22 @@ __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int
             prev_a = col;
             prev_m = mcol;
         }
-    } else if (warp != 4) {
+    } else if (warp == 4) {
+        for (int k = 0; k < nb; ++k) {
+            nbar_sync(1 + (k & 1), kPipe);  // READY(k)
+            if (mt != nullptr) {
+                mt[k * kTile + lane] = S.x[lane][k];
+                if (lane == 0) dv[k] = S.yv[k];
+            }
+            if (k + 2 < nb) nbar_arrive(3 + (k & 1), kPipe);  // UPD(k)
+            // publish every eighth column, every second one near the end
+            if (mt != nullptr && ((k & 7) == 7 || (k >= 24 && (k & 1)) || k == nb - 1)) {
+                __threadfence();
+                __syncwarp();
+                if (lane == 0) atomicExch(colcount, col_base + (unsigned)k + 1u);
+            }
+        }
+    } else {
         const int wid = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;  // 0..191
         for (int k = 0; k < nb; ++k) {
             nbar_sync(1 + (k & 1), kPipe);  // READY(k)
@@ -359,42 +382,20 @@ __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int
     if (tid == 0 && S.fail != 0 && info != nullptr) atomicCAS(info, 0, (int32_t)(row0 + S.fail));
 }
 
-// From M (strict lower, in m) and the pivots d (in dv): the tile's
-// L = M diag(d)^{1/2} into `tile` (upper part and zero_right columns set
-// to zero) and L^{-1} = diag(d)^{-1/2} M^{-1} into `tinv`.  M^{-1}: its
-// 8 x 8 diagonal blocks by substitution (one column per thread), then
-// recursive doubling.  z and u are scratch.
+// The tile's L = M diag(d)^{1/2} from M (strict lower, in m) and the
+// pivots d (in dv) into `tile`, the upper part and the zero_right columns
+// to the right of the tile set to zero.
 template <typename T>
-__device__ void tile_outputs_from_m(T (*m)[kTile + 1], const T* dv, T (*z)[kTile + 1], T (*u)[kTile + 1], T* rs,
-                                    T* tile, int64_t ld, int nb, int zero_right, T* tinv) {
+__device__ void tile_l_from_m(T (*m)[kTile + 1], const T* dv, T* tile, int64_t ld, int nb, int zero_right) {
     const int tid = threadIdx.x;
-    for (int e = tid; e < kTile * kTile; e += kTileThreads) z[e / kTile][e % kTile] = T(0);
-    if (tid < kTile) rs[tid] = rsq<T>(dv[tid]);
-    __syncthreads();
-    if (tid < kTile) {  // column c of the inverse of c's 8-block
-        const int c = tid, b0 = c & ~7;
-        z[c][c] = T(1);
-        for (int i = c + 1; i < b0 + 8; ++i) {
-            T acc = m[i][c];
-            for (int k = c + 1; k < i; ++k) acc = fma(m[i][k], z[k][c], acc);
-            z[i][c] = -acc;
-        }
-    }
-    __syncthreads();
-    unit_inverse_doubling<T>(m, z, u);
-    for (int e = tid; e < kTile * kTile; e += kTileThreads) {
-        const int r = e / kTile, c = e % kTile;
-        if (r >= nb || c >= nb) continue;
-        T lv = T(0), xv = T(0);
-        if (c < r) {
-            lv = m[r][c] * (dv[c] * rs[c]);
-            xv = z[r][c] * rs[r];
-        } else if (c == r) {
-            lv = dv[r] * rs[r];
-            xv = rs[r];
+    for (int e = tid; e < nb * nb; e += kTileThreads) {
+        const int r = e / nb, c = e - (e / nb) * nb;
+        T lv = T(0);
+        if (c <= r) {
+            const T sq = dv[c] * rsq<T>(dv[c]);  // sqrt(d_c)
+            lv = (c < r) ? m[r][c] * sq : sq;
         }
         tile[(int64_t)r * ld + c] = lv;
-        tinv[r * kTile + c] = xv;
     }
     for (int e = tid; e < nb * zero_right; e += kTileThreads) {
         const int r = e / zero_right, c = e % zero_right;
