@@ -65,6 +65,9 @@ def parse():
     p.add_argument("--cpu-sample-blocks", type=int, default=32)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--bare", action="store_true",
+                   help="only the warm-up and timed steps (for profiler launch lists): no comparison form, "
+                        "no accuracy run, no live FP64 peak, no e2e, no CPU baseline")
     p.add_argument("--workload", choices=["bta", "batched", "kappa", "autograd"], default="bta")
     p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--batch-precision", choices=["native", "mixed"], default="native")
@@ -291,6 +294,8 @@ def bench_ours(args, rank: int, world: int, dist):
 
     # the comparison forms (e.g. the FP64 drop-in beside the mixed form)
     compare = {}
+    if args.bare:
+        args.compare, args.no_e2e, args.no_cpu_baseline = "", True, True
     for cp in [c for c in args.compare.split(",") if c and c != prec]:
         Ac = [x.clone() for x in A0]
         ps, _, pr, _ = _timed_sweeps(torch, sg, _lib, Ac, A0, cp, max(1, args.steps // 2), 1, local, dist)
@@ -301,7 +306,7 @@ def bench_ours(args, rank: int, world: int, dist):
     # accuracy statement: a mixed form is compared with this GPU's FP64 path
     # (which the test suite pins to the reference at <= 1e-12)
     acc = {}
-    if prec.startswith("mixed"):
+    if prec.startswith("mixed") and not args.bare:
         ref = [x.clone() for x in A0]
         sg.pobtaf(*ref)
         sg.pobtasi(*ref)
@@ -312,7 +317,7 @@ def bench_ours(args, rank: int, world: int, dist):
     else:
         acc = {"note": "FP64 path; parity with the reference pinned at <=1e-12 by the test suite"}
 
-    roof = _roofline(torch, prof)
+    roof = None if args.bare else _roofline(torch, prof)
 
     # end to end through the public API with pinned host arrays
     e2e = None

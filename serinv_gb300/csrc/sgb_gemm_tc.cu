@@ -54,6 +54,7 @@ constexpr int TC_BM = 128;
 constexpr int TC_BK = 32;
 constexpr int kMaxTcProbs = 4;
 constexpr int64_t kTcSmCount = 148;  // CTAs one launch should keep busy (152 SMs)
+constexpr int kTcMaxSplit = 4;      // CTAs per cluster of a K-split tile
 constexpr int kMaxSplitJobs = 2 * kMaxTcProbs;  // probs x operands
 constexpr long long kSpinLimit = 1ll << 22;         // bounded mbarrier waits (~1 s)
 
@@ -80,8 +81,8 @@ struct SplitJob {
     int32_t strips, strip_begin;  // kSplitRows-row strips per instance; first CTA of the job
 };
 
-constexpr int kSplitRows = 8;
-constexpr int kSplitThreads = 512;  // four warps per scheduler: the split is latency bound
+constexpr int kSplitRows = 4;
+constexpr int kSplitThreads = 512;  // two CTAs per SM, eight warps per scheduler: latency bound
 constexpr int kSplitLd = kTcMaxK + 1;  // odd stride: conflict-free row and column access
 
 struct SplitLaunch {
@@ -113,13 +114,27 @@ __device__ __forceinline__ void digits(double x, int Erow, int (&d)[S]) {
     else if (rs <= 0) X = m << (-rs);
     else X = (m + (1ll << (rs - 1))) >> rs;
     if (bits >> 63) X = -X;
+    // |X| < 2^(7S+1) <= 2^50: the low L digits come out of the low 7L bits
+    // and the rest out of the high part, all in 32-bit arithmetic (the
+    // balanced digit v = ((x mod 128) ^ 64) - 64 lies in [-64, 63]; removing
+    // the low digits leaves a carry of 0 or 1 for the high part).
+    constexpr int L = (S - 1) < 3 ? (S - 1) : 3;
+    int lo = (int)(X & ((1ll << (7 * L)) - 1));
+    int hi = (int)(X >> (7 * L));
 #pragma unroll
-    for (int p = S - 1; p >= 1; --p) {
-        const int v = ((int)(X & 127) ^ 64) - 64;  // balanced digit in [-64, 63]
+    for (int p = S - 1; p >= S - L; --p) {
+        const int v = ((lo & 127) ^ 64) - 64;
         d[p] = v;
-        X = (X - v) >> 7;
+        lo = (lo - v) >> 7;
     }
-    d[0] = (int)X;
+    hi += lo;
+#pragma unroll
+    for (int p = S - L - 1; p >= 1; --p) {
+        const int v = ((hi & 127) ^ 64) - 64;
+        d[p] = v;
+        hi = (hi - v) >> 7;
+    }
+    d[0] = hi;
 }
 
 // One CTA per strip of kSplitRows rows of one operand instance: the whole
@@ -140,38 +155,45 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(const __grid_constant__
     // Each source covers [koff, koff + Kp) of the strip (Kp = K rounded up to
     // 32); elements past K or past the last row are written as zeros, so
     // every element of the strip is written once.  A thread issues all its
-    // loads (at most kSplitPer) before it stores any, so a CTA keeps its
-    // whole strip in flight at once.
-    constexpr int kSplitPer = kSplitRows * kTcMaxK / kSplitThreads;
+    // loads before it stores any (no index division: rows of a row-major
+    // source are walked by consecutive threads, a transposed source by four
+    // rows times 128 k per pass).
     for (int q = 0; q < J.nsrc; ++q) {
         const SplitSrc& src = J.src[q];
         const double* X = src.X + (int64_t)inst * src.stride;
         const int Kp = (src.K + TC_BK - 1) / TC_BK * TC_BK;
-        const int total = kSplitRows * Kp;
-        const bool rowmajor = src.ld_k == 1;  // else columns contiguous in r
-        for (int e0 = tid; e0 < total; e0 += kSplitThreads * kSplitPer) {
-            double v[kSplitPer];
-            int dst[kSplitPer];
+        if (src.ld_k == 1) {
+            constexpr int KU = (kTcMaxK + kSplitThreads - 1) / kSplitThreads;  // 2
+            double v[kSplitRows][KU];
 #pragma unroll
-            for (int u = 0; u < kSplitPer; ++u) {
-                const int e = e0 + u * kSplitThreads;
-                int rr, k;
-                if (rowmajor) {  // a warp reads 32 consecutive k of one row
-                    rr = e / Kp;
-                    k = e - rr * Kp;
-                } else {  // eight rows of four k per warp
-                    k = e / kSplitRows;
-                    rr = e % kSplitRows;
+            for (int rr = 0; rr < kSplitRows; ++rr)
+#pragma unroll
+                for (int u = 0; u < KU; ++u) {
+                    const int k = tid + u * kSplitThreads, r = r0 + rr;
+                    v[rr][u] = (k < src.K && r < J.R) ? __ldg(X + (int64_t)r * src.ld_r + k) : 0.0;
                 }
-                const int r = r0 + rr;
-                const bool in = e < total;
-                const bool load = in && r < J.R && k < src.K;
-                dst[u] = in ? rr * kSplitLd + src.koff + k : -1;
-                v[u] = load ? __ldg(X + (int64_t)r * src.ld_r + (int64_t)k * src.ld_k) : 0.0;
+#pragma unroll
+            for (int rr = 0; rr < kSplitRows; ++rr)
+#pragma unroll
+                for (int u = 0; u < KU; ++u) {
+                    const int k = tid + u * kSplitThreads;
+                    if (k < Kp) t[rr][src.koff + k] = v[rr][u];
+                }
+        } else {
+            constexpr int KS = kSplitThreads / kSplitRows;  // 128 k per pass
+            constexpr int KU = (kTcMaxK + KS - 1) / KS;     // 5
+            const int rr = tid % kSplitRows, r = r0 + rr;
+            double v[KU];
+#pragma unroll
+            for (int u = 0; u < KU; ++u) {
+                const int k = tid / kSplitRows + u * KS;
+                v[u] = (k < src.K && r < J.R) ? __ldg(X + (int64_t)r * src.ld_r + (int64_t)k * src.ld_k) : 0.0;
             }
 #pragma unroll
-            for (int u = 0; u < kSplitPer; ++u)
-                if (dst[u] >= 0) (&t[0][0])[dst[u]] = v[u];
+            for (int u = 0; u < KU; ++u) {
+                const int k = tid / kSplitRows + u * KS;
+                if (k < Kp) t[rr][src.koff + k] = v[u];
+            }
         }
     }
     if (J.nsrc == 0)
@@ -601,27 +623,41 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         r_lo = (int)(rank * TC_BM / ks);
         r_hi = (int)((rank + 1) * TC_BM / ks);
         const int nr = r_hi - r_lo;
-        uint32_t rb[8];
+        uint32_t rb[kTcMaxSplit];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) rb[q] = q < ks ? dsmem_addr(smem_u32(R), (uint32_t)q) : 0u;
+        for (int q = 0; q < kTcMaxSplit; ++q) rb[q] = q < ks ? dsmem_addr(smem_u32(R), (uint32_t)q) : 0u;
+        // two elements per pass, all their remote loads in flight together
 #pragma unroll 1
-        for (int e = tid; e < nr * BN; e += TC_THREADS2) {
-            const int row = r_lo + e % nr, col = e / nr;
-            float acc[NACC][8];
+        for (int e = tid; e < nr * BN; e += 2 * TC_THREADS2) {
+            float acc[2][NACC][kTcMaxSplit];
 #pragma unroll
-            for (int l = 0; l < NACC; ++l)
+            for (int hh = 0; hh < 2; ++hh) {
+                const int eh = e + hh * TC_THREADS2;
+                const int row = r_lo + eh % nr, col = eh / nr;
+                const bool in = eh < nr * BN;
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    acc[l][q] = q < ks ? ld_dsmem(rb[q] + (uint32_t)(((l * BN + col) * TC_BM + row) * 4)) : 0.f;
-            float vv[NACC];
+                for (int l = 0; l < NACC; ++l)
 #pragma unroll
-            for (int l = 0; l < NACC; ++l) {
-                float t = 0.f;
-#pragma unroll
-                for (int q = 0; q < 8; ++q) t += acc[l][q];
-                vv[l] = t;
+                    for (int q = 0; q < kTcMaxSplit; ++q)
+                        acc[hh][l][q] = (in && q < ks)
+                                            ? ld_dsmem(rb[q] + (uint32_t)(((l * BN + col) * TC_BM + row) * 4))
+                                            : 0.f;
             }
-            Ds[(row - r_lo) * (BN + 1) + col] = combine(vv, eAs[row], eBs[col]);
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+                const int eh = e + hh * TC_THREADS2;
+                if (eh >= nr * BN) break;
+                const int row = r_lo + eh % nr, col = eh / nr;
+                float vv[NACC];
+#pragma unroll
+                for (int l = 0; l < NACC; ++l) {
+                    float t = 0.f;
+#pragma unroll
+                    for (int q = 0; q < kTcMaxSplit; ++q) t += acc[hh][l][q];
+                    vv[l] = t;
+                }
+                Ds[(row - r_lo) * (BN + 1) + col] = combine(vv, eAs[row], eBs[col]);
+            }
         }
     } else {
         Ds = (double*)smem;
@@ -782,7 +818,7 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
     int ks = 1;
     if (tiles64 > 0 && tiles64 < 100) {
         int64_t k = kTcSmCount / tiles64;
-        if (k > 8) k = 8;
+        if (k > kTcMaxSplit) k = kTcMaxSplit;
         if (k > minkb) k = minkb;
         ks = k < 1 ? 1 : (int)k;
     }
