@@ -301,22 +301,44 @@ __device__ void factor_tile(Smem<T>& S, T* tile, int64_t ld, int nb, int zero_ri
     __syncthreads();
 }
 
-// The pipeline part of factor_tile alone: after it, S.x holds the strict
-// lower part of M (zero elsewhere) and S.yv the pivots d (1 beyond nb), so
-// L = M diag(d)^{1/2}.  No inverse, no output.  With `mt` set, warp 4
-// publishes the factor column by column while the pipeline runs: column k
-// of M to mt[k][0..31] (transposed, so a column is one coalesced row) and
-// d_k to dv[k]; every eight columns (every second one from column 24, and
-// after the last) it makes them visible at GPU scope and sets
-// *colcount = col_base + k + 1, so other CTAs can consume the columns as
-// they appear.  Warp 4 takes part in the READY/UPD barriers like a worker
-// either way (it does no FP64 work).
+// The pipeline part of factor_tile alone, for the persistent column-block
+// kernel: after it, S.x holds the strict lower part of M (zero elsewhere)
+// and S.yv the pivots d (1 beyond nb), so L = M diag(d)^{1/2}; no inverse,
+// no output.  The sequential chain is split between two warps on different
+// SM quarters so that each carries as few FP64 instructions as possible:
+//
+// * warp 0 (pivot) keeps only the pivots: from 1/d_j and the pair
+//   (q_{j+1}, e_{j+1}) = (a'_{j+1,j}^2, diagonal of column j+1 through
+//   column j-1) it forms d_{j+1} = e_{j+1} - q_{j+1} / d_j with one FMA, tests
+//   it and takes its reciprocal (three FMAs after an FP32 seed): four FP64
+//   instructions per column;
+// * warp 1 (companion) keeps column j of a' in registers: with 1/d_j it
+//   forms M(:, j), publishes the column (READY), updates column j+1 with
+//   column j and the diagonal with column j (registers), and hands the
+//   pivot warp (q_{j+2}, e_{j+2}) -- four FP64 instructions per column;
+// * warps 2, 3, 6, 7 (quarters 2 and 3) apply column k to the strict lower
+//   part of columns k+2.. (the companion keeps the diagonal), then UPD;
+// * with `mt` set, warp 4 publishes the factor column by column: column k
+//   of M to mt[k][0..31] (transposed, so a column is one coalesced row) and
+//   d_k to dv[k]; every eight columns (every second one from column 24, and
+//   after the last) it makes them visible at GPU scope and sets
+//   *colcount = col_base + k + 1, so other CTAs can consume the columns as
+//   they appear.  It takes part in READY/UPD either way (no FP64 work).
+//
+// Pivot <-> companion hand-offs use named barriers PQ (ids 5, 6) and QP
+// (7, 8), READY/UPD ids 1-4; every pair alternates between two ids so that
+// no side can run two generations ahead (the arrival sequence was checked
+// on a CPU model for nb = 1..32).
 template <typename T>
 __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int32_t* info, int64_t row0,
                               T* mt = nullptr, T* dv = nullptr, unsigned* colcount = nullptr,
                               unsigned col_base = 0) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr int kPipe = kTileThreads;  // pivot warp + six worker warps + warp 4
+    constexpr int kCons = 32 * 6;  // companion + four workers + publisher
+    constexpr int kPair = 64;
+    T* iv = &S.tmp[0][0];  // 1/d_j
+    T* qv = &S.tmp[1][0];  // a'_{j,j-1}^2
+    T* ev = &S.tmp[2][0];  // diagonal of column j through column j-2
     for (int e = tid; e < kTile * kTile; e += kTileThreads) {
         const int r = e / kTile, c = e % kTile;
         T v = T(0);
@@ -324,39 +346,70 @@ __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int
         else if (r >= nb && r == c) v = T(1);
         S.s[r][c] = v;
         S.x[r][c] = T(0);
-        if (c <= r) S.tri[r * (r + 1) / 2 + c] = (unsigned short)((r << 8) | c);
+        if (c < r) S.tri[r * (r - 1) / 2 + c] = (unsigned short)((r << 8) | c);  // strict lower, row-major
     }
     if (tid < kTile) S.yv[tid] = T(1);
     if (tid == 0) S.fail = 0;
     __syncthreads();
     if (warp == 0) {
-        T prev_a = T(0), prev_m = T(0);
+        T d = S.s[0][0];
+        bool ok = pivot_ok(d);
+        T inv = ok ? rcp_pivot(d) : T(NAN);
+        if (lane == 0 && !ok) S.fail = 1;
         for (int j = 0; j < nb; ++j) {
-            if (j >= 2) nbar_sync(3 + (j & 1), kPipe);  // UPD(j-2)
-            T col = S.s[lane][j];
-            if (j >= 1) col = fma(-prev_a, __shfl_sync(0xffffffffu, prev_m, j), col);
-            const T d = __shfl_sync(0xffffffffu, col, j);
-            const bool ok = pivot_ok(d);
-            const T inv = ok ? rcp_pivot(d) : T(NAN);
+            if (lane == 0) {
+                S.yv[j] = d;
+                iv[j] = inv;
+            }
+            nbar_arrive(5 + (j & 1), kPair);  // PQ(j)
+            if (j + 1 < nb) {
+                nbar_sync(7 + ((j - 1) & 1), kPair);  // QP(j-1): q_{j+1}, e_{j+1}
+                d = fma(-qv[j + 1], inv, ev[j + 1]);
+                ok = pivot_ok(d);
+                inv = ok ? rcp_pivot(d) : T(NAN);
+                if (lane == 0 && !ok && S.fail == 0) S.fail = j + 2;
+            }
+        }
+    } else if (warp == 1) {
+        T col = S.s[lane][0];
+        T diag = S.s[lane][lane];
+        if (nb >= 2) {
+            if (lane == 1) {
+                qv[1] = col * col;
+                ev[1] = diag;
+            }
+            nbar_arrive(8, kPair);  // QP(-1)
+        }
+        for (int j = 0; j < nb; ++j) {
+            nbar_sync(5 + (j & 1), kPair);  // PQ(j)
+            const T inv = iv[j];
             const T mcol = col * inv;
             if (lane >= j) S.s[lane][j] = col;
             if (lane > j) S.x[lane][j] = mcol;
-            if (lane == j) {
-                S.yv[j] = d;
-                if (!ok && S.fail == 0) S.fail = j + 1;
+            nbar_arrive(1 + (j & 1), kCons);  // READY(j)
+            if (j >= 1) nbar_sync(3 + ((j - 1) & 1), kCons);  // UPD(j-1)
+            if (j + 1 < nb) {
+                const T mj1 = __shfl_sync(0xffffffffu, mcol, j + 1);
+                const T col1 = fma(-col, mj1, S.s[lane][j + 1]);  // column j+1 through column j
+                diag = fma(-col, mcol, diag);                      // diagonal through column j
+                if (j + 2 < nb) {
+                    if (lane == j + 2) {
+                        qv[j + 2] = col1 * col1;
+                        ev[j + 2] = diag;
+                    }
+                    nbar_arrive(7 + (j & 1), kPair);  // QP(j)
+                }
+                col = col1;
             }
-            nbar_arrive(1 + (j & 1), kPipe);  // READY(j)
-            prev_a = col;
-            prev_m = mcol;
         }
     } else if (warp == 4) {
         for (int k = 0; k < nb; ++k) {
-            nbar_sync(1 + (k & 1), kPipe);  // READY(k)
+            nbar_sync(1 + (k & 1), kCons);  // READY(k)
             if (mt != nullptr) {
                 mt[k * kTile + lane] = S.x[lane][k];
                 if (lane == 0) dv[k] = S.yv[k];
             }
-            if (k + 2 < nb) nbar_arrive(3 + (k & 1), kPipe);  // UPD(k)
+            if (k + 1 < nb) nbar_arrive(3 + (k & 1), kCons);  // UPD(k)
             // publish every eighth column, every second one near the end
             if (mt != nullptr && ((k & 7) == 7 || (k >= 24 && (k & 1)) || k == nb - 1)) {
                 __threadfence();
@@ -364,18 +417,18 @@ __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int
                 if (lane == 0) atomicExch(colcount, col_base + (unsigned)k + 1u);
             }
         }
-    } else {
-        const int wid = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;  // 0..191
+    } else if (warp != 5) {
+        const int wid = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;  // 0..127
         for (int k = 0; k < nb; ++k) {
-            nbar_sync(1 + (k & 1), kPipe);  // READY(k)
+            nbar_sync(1 + (k & 1), kCons);  // READY(k)
             const int w = nb - k - 2;
-            const int n1 = w > 0 ? w * (w + 1) / 2 : 0;
-            for (int e = wid; e < n1; e += 192) {  // rank-1 update of columns k+2..
+            const int n1 = w > 1 ? w * (w - 1) / 2 : 0;
+            for (int e = wid; e < n1; e += 128) {  // column k on the strict lower part of columns k+2..
                 const int rc = S.tri[e];
                 const int r = k + 2 + (rc >> 8), c = k + 2 + (rc & 0xff);
                 S.s[r][c] = fma(-S.s[r][k], S.x[c][k], S.s[r][c]);
             }
-            if (k + 2 < nb) nbar_arrive(3 + (k & 1), kPipe);  // UPD(k)
+            if (k + 1 < nb) nbar_arrive(3 + (k & 1), kCons);  // UPD(k)
         }
     }
     __syncthreads();
