@@ -56,10 +56,15 @@ class _Arr:
         if self.kind == "devcopy":
             self.src.copy_(self.t)
         elif self.kind == "torch_host":
-            self.src.copy_(self.t.to("cpu"))
+            # straight into the caller's memory (one DMA when it is pinned);
+            # the caller's stream is synchronized before returning
+            self.src.copy_(self.t, non_blocking=True)
         elif self.kind == "numpy":
-            host = self.t.to("cpu").numpy()
-            np.copyto(self.src, host.reshape(self.src.shape), casting="no")
+            if self.src.flags.c_contiguous:
+                torch.from_numpy(self.src).copy_(self.t.view(self.src.shape), non_blocking=True)
+            else:
+                host = self.t.to("cpu").numpy()
+                np.copyto(self.src, host.reshape(self.src.shape), casting="no")
 
 
 def _device_of(arrs) -> torch.device:
@@ -79,11 +84,13 @@ def _wrap(x, device: torch.device, name: str) -> _Arr:
             if x.is_contiguous():
                 return _Arr(x, x, "dev")
             return _Arr(x.contiguous(), x, "devcopy")
-        return _Arr(x.to(device).contiguous(), x, "torch_host")
+        # asynchronous from pinned memory, ordered before the library's
+        # kernels on the same stream
+        return _Arr(x.to(device, non_blocking=True).contiguous(), x, "torch_host")
     if isinstance(x, np.ndarray):
         if not x.flags.writeable:
             raise ValueError(f"{name} is read-only; the computation is in place")
-        return _Arr(torch.from_numpy(np.ascontiguousarray(x)).to(device), x, "numpy")
+        return _Arr(torch.from_numpy(np.ascontiguousarray(x)).to(device, non_blocking=True), x, "numpy")
     if hasattr(x, "__dlpack__"):
         t = torch.from_dlpack(x)
         if not t.is_cuda:

@@ -62,12 +62,6 @@ struct Ctx {
     int32_t* status = nullptr;  // device status word (SGB_ERR_TIMEOUT on a stuck wait)
 };
 
-// Mixed pobtaf: factor [D_i; Lo_i; Ar_i] with the tall-panel sweep (false),
-// or factor D_i alone, invert it and run the TRSMs on the tensor cores
-// (true).  The second moves the TRSM flops to the tensor cores but needs a
-// triangular inversion per block (two dozen small launches), which costs
-// more than it saves at b = 512 on the launch-bound diagonal chain.
-constexpr bool kMixedInverseTrsm = false;
 
 // Upper bound of the tensor-core scratch of one grouped launch with up to
 // `nprob` problems whose sizes are at most mx x mx and K at most kmax.
@@ -162,22 +156,17 @@ struct Carve {
 
 template <typename T>
 struct PobtafWs {
-    size_t status, bar, tinv, tc, tc_bytes, linv, trtri, total;
+    size_t status, bar, tinv, tc, tc_bytes, xinv, total;
     PobtafWs(const sgb_bta* m, int S = 0) {
         Carve c;
         status = c.take(256);
         bar = c.take(256);
         tinv = c.take(sizeof(T) * (4 * kTile * kTile + 2 * kTile));  // column-block kernel scratch
         const int64_t mx = m->b > m->a ? m->b : m->a;
-        tc_bytes = 0;
-        if (S) {
-            const size_t g = tc_bound(S, mx, m->b, 3), t1 = trtri_tc_bytes(S, m->b, 1);
-            tc_bytes = g > t1 ? g : t1;
-        }
+        tc_bytes = S ? tc_bound(S, mx, m->b, 3) : 0;
         tc = c.take(tc_bytes);
-        // mixed precision only: L_ii^{-1} and its triangular-inverse scratch
-        linv = c.take(S ? sizeof(T) * m->b * m->b : 0);
-        trtri = c.take(S ? sizeof(T) * trtri_scratch_elems(m->b, 1) : 0);
+        // mixed precision only: L_ii^{-T} of the current diagonal block
+        xinv = c.take(S ? sizeof(T) * m->b * m->b : 0);
         total = c.off;
     }
 };
@@ -308,46 +297,51 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
     cx.tc_bytes = L.tc_bytes;
     cx.status = (int32_t*)((char*)ws + L.status);
     const int64_t bb = b * b, ab = a * b;
-    T* Linv = (T*)((char*)ws + L.linv);
-    T* trs = (T*)((char*)ws + L.trtri);
+    T* Xinv = (T*)((char*)ws + L.xinv);
 
-    // [D_i; rows below] <- Cholesky of the column block.  Native: one blocked
-    // sweep over the tall column block (the TRSMs fold into the rank-32
-    // updates).  Mixed: only D_i is factored on the FP64 pipe; its inverse
-    // is formed and the TRSMs run as tensor-core products with L_ii^{-T}.
+    // [D_i; rows below] <- Cholesky of the column block.  Native: one
+    // blocked sweep over the tall column block (the TRSMs fold into the
+    // rank-32 updates).  Mixed: the persistent launch factors D_i alone and
+    // forms L_ii^{-T} on the FP64 pipe; the rows below become one
+    // tensor-core product rows * L_ii^{-T}.
     unsigned* bar = (unsigned*)((char*)ws + L.bar);
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     SGB_TRY(cudaStreamIsCapturing(s, &cap));
     // one cooperative launch per block, except under stream capture (graph
     // plans) and for small blocks, where the launch-based sweep is used
     const bool persistent = cap == cudaStreamCaptureStatusNone && b > 2 * kTile;
+    bool mixed_inverse = S != 0 && persistent;
+    // the launch writes only the upper block triangle of L_ii^{-T}
+    if (mixed_inverse) SGB_TRY(cudaMemsetAsync(Xinv, 0, sizeof(T) * bb, s));
     auto factor = [&](int64_t i, RowSet<T> r1, RowSet<T> r2) -> int {
         T* Di = D + i * bb;
-        if (S == 0 || !kMixedInverseTrsm) {
-            cudaError_t e = persistent
-                                ? factor_panel_persistent<T>(Di, b, b, r1, r2, tinv, bar, cx.status, info, i * b, s)
-                                : cudaErrorNotSupported;
-            if (e == cudaErrorNotSupported) e = factor_column_block<T>(Di, b, b, r1, r2, tinv, info, i * b, s);
-            return e == cudaSuccess ? SGB_OK : cuda_fail(e);
+        if (mixed_inverse) {
+            RowSet<T> none{nullptr, 0, b};
+            cudaError_t e = factor_panel_persistent<T>(Di, b, b, none, none, tinv, bar, cx.status, info, i * b, s, Xinv);
+            if (e == cudaSuccess) {
+                GemmProb<T> pr[2];
+                int np = 0;
+                for (RowSet<T> r : {r1, r2}) {
+                    if (r.rows <= 0) continue;
+                    GemmProb<T> p = prob<T>();  // rows <- rows * L_ii^{-T}, in place (operands are sliced first)
+                    p.M = (int32_t)r.rows;
+                    p.N = (int32_t)b;
+                    set_term<T>(p, 0, r.p, r.ld, 0, Xinv, b, 0, b, KM_LT_N1);
+                    p.Cout = r.p;
+                    p.ldc = r.ld;
+                    pr[np++] = p;
+                }
+                if (np) SGB_TRY(run_gemm<T>(cx, pr, np, s));
+                return SGB_OK;
+            }
+            if (e != cudaErrorNotSupported) return cuda_fail(e);
+            mixed_inverse = false;  // too few SMs for the persistent launch
         }
-        RowSet<T> none{nullptr, 0, b};
-        cudaError_t e = factor_column_block<T>(Di, b, b, none, none, tinv, info, i * b, s);
-        if (e == cudaSuccess) e = trtri_run<T>(cx, Di, b, 1, Linv, trs, s);
-        if (e != cudaSuccess) return cuda_fail(e);
-        GemmProb<T> pr[2];
-        int np = 0;
-        for (RowSet<T> r : {r1, r2}) {
-            if (r.rows <= 0) continue;
-            GemmProb<T> p = prob<T>();  // rows <- rows * L_ii^{-T}, in place (operands are sliced first)
-            p.M = (int32_t)r.rows;
-            p.N = (int32_t)b;
-            set_term<T>(p, 0, r.p, r.ld, 0, Linv, b, 1, b, KM_LT_N1);
-            p.Cout = r.p;
-            p.ldc = r.ld;
-            pr[np++] = p;
-        }
-        if (np) SGB_TRY(run_gemm<T>(cx, pr, np, s));
-        return SGB_OK;
+        cudaError_t e = persistent
+                            ? factor_panel_persistent<T>(Di, b, b, r1, r2, tinv, bar, cx.status, info, i * b, s)
+                            : cudaErrorNotSupported;
+        if (e == cudaErrorNotSupported) e = factor_column_block<T>(Di, b, b, r1, r2, tinv, info, i * b, s);
+        return e == cudaSuccess ? SGB_OK : cuda_fail(e);
     };
 
     for (int64_t i = 0; i < n - 1; ++i) {

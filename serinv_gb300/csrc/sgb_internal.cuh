@@ -103,13 +103,17 @@ template <typename T>
 using GemmFn = cudaError_t (*)(void* ctx, GemmProb<T>* probs, int np, cudaStream_t s);
 
 // The same column-block factorization as one cooperative persistent launch
-// (sgb_panel.cu).  `bar` is two unsigned words of scratch; `status` receives
-// SGB_ERR_TIMEOUT if a grid barrier gives up.  Not for use under stream
-// capture (cooperative launch).
+// (sgb_panel.cu).  `bar` is 16 unsigned words of scratch; `status` receives
+// SGB_ERR_TIMEOUT if a grid barrier gives up.  With `xinv` (m x m,
+// row-major, ld m) the launch also writes L^{-T} there: its upper block
+// triangle including the diagonal tiles (zeros below the diagonal inside
+// them); the tiles strictly below the diagonal tiles are not written, so
+// the caller zeroes them once.  Not for use under stream capture
+// (cooperative launch).
 template <typename T>
 cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, RowSet<T> r2, T* tinv,
                                     unsigned* bar, int32_t* status, int32_t* info, int64_t info_row0,
-                                    cudaStream_t s);
+                                    cudaStream_t s, T* xinv = nullptr);
 
 // Full triangular inverse of `batch` lower-triangular m x m blocks:
 // Linv_j = L_j^{-1} (zeros above the diagonal).  Scratch: batch*m*m T.

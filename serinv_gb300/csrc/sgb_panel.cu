@@ -60,6 +60,8 @@ struct PanelArgs {
     int64_t r1rows, r1ld;
     T* r2;
     int64_t r2rows, r2ld;
+    T* xinv;  // m x m, row-major (ld xld): L^{-T} out, or null
+    int64_t xld;
     T* scratch;  // [2][32][32] (unused), [2][32][32] M^T by column, [2][32] d
     int32_t* info;
     int64_t row0;
@@ -154,13 +156,15 @@ __device__ __forceinline__ T* row_ptr(const PanelArgs<T>& a, int64_t c1, int64_t
 // column; one shuffle and one FMA per column), X = Y diag(d)^{-1/2}.  The
 // columns of M (transposed in mt) and the pivots dv are consumed as the
 // factorizer publishes them: column k once *colcount >= col_base + k + 1
-// (bounded wait), all available columns loaded at once.  Returns false on a
+// (bounded wait), all available columns loaded at once.  With unit >= 0
+// the row is the unit vector e_unit instead of the stored values (a row of
+// the identity, whose solve is a row of L^{-T}).  Returns false on a
 // timeout or an error raised elsewhere.
 template <typename T>
 __device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T* dv, const unsigned* colcount,
-                                              unsigned col_base, int32_t* status) {
+                                              unsigned col_base, int32_t* status, int unit = -1) {
     const int tx = threadIdx.x & 31;
-    T y = tx < w ? ldcg(rp + tx) : T(0);
+    T y = tx < w ? (unit >= 0 ? T(tx == unit ? 1 : 0) : ldcg(rp + tx)) : T(0);
     int k = 0;
     long long spins = 0;
     while (k < w) {
@@ -345,20 +349,33 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         // ---------------- workers
         // B(p): the rows below tile p except tile-row p+1 (the helpers'),
         // one row per warp, following the published columns of M
+        // and, with xinv, the rows of L^{-T} that are not zero in column
+        // block p (rows < c1; those of tile-row p start as identity rows)
         const unsigned nwk = G - kW0, wk = cta - kW0;
         const int64_t off0 = w2;
-        const int64_t nrows = (m - c1) + a.r1rows + a.r2rows - off0;
-        for (int64_t r = (int64_t)wk * 8 + ty; r < nrows; r += (int64_t)nwk * 8)
-            if (!trsm_row_pipe<T>(row_ptr(a, c1, off0 + r) + c0, w, Mp, dp, CC, (unsigned)(p * kTile), a.status))
-                break;
+        const int64_t nbase = (m - c1) + a.r1rows + a.r2rows - off0;
+        const int64_t nrows = nbase + (a.xinv ? c1 : 0);
+        for (int64_t r = (int64_t)wk * 8 + ty; r < nrows; r += (int64_t)nwk * 8) {
+            T* rp;
+            int unit = -1;
+            if (r < nbase) {
+                rp = row_ptr(a, c1, off0 + r) + c0;
+            } else {
+                const int64_t xr = r - nbase;
+                rp = a.xinv + xr * a.xld + c0;
+                if (xr >= c0) unit = (int)(xr - c0);
+            }
+            if (!trsm_row_pipe<T>(rp, w, Mp, dp, CC, (unsigned)(p * kTile), a.status, unit)) break;
+        }
         if (!has_next) break;
         if (!group_barrier(barB, G - 2, epB, a.status, &S.flag)) return;
 
         // C(p): rank-w update of the trailing panel without tile-rows p+1, p+2
         const int64_t ntd = (m - c1 + kTile - 1) / kTile;
         const int64_t n1 = (a.r1rows + kTile - 1) / kTile, n2 = (a.r2rows + kTile - 1) / kTile;
+        const int64_t nx = a.xinv ? p + 1 : 0;  // tile-rows of L^{-T} not zero in block p
         const int64_t tiles_d = ntd * (ntd + 1) / 2;
-        const int64_t total = tiles_d + (n1 + n2) * ntd;
+        const int64_t total = tiles_d + (n1 + n2 + nx) * ntd;
         const int64_t t0 = tiles_d < 3 ? tiles_d : 3;
         const T* Bpan = a.diag + c1 * a.ldd + c0;
         // Tile t's operands are staged in one of two shared buffers while
@@ -367,9 +384,11 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
             T* C;
             const T* A;
             int64_t ldc, rows, cols, cj;
+            bool fresh;  // C holds no value yet (L^{-T} tile-row p): C = -update
         };
         auto tile_ref = [&](int64_t t) {
             TileRef R;
+            R.fresh = false;
             int64_t ti;
             if (t < tiles_d) {  // lower tiles of the trailing D, row-major over the triangle
                 ti = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
@@ -388,7 +407,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                 R.A = a.r1 + ti * kTile * a.r1ld + c0;
                 R.ldc = a.r1ld;
                 R.rows = a.r1rows - ti * kTile;
-            } else {
+            } else if (t < tiles_d + (n1 + n2) * ntd) {
                 const int64_t u = t - tiles_d - n1 * ntd;
                 ti = u / ntd;
                 R.cj = u % ntd;
@@ -396,6 +415,15 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                 R.A = a.r2 + ti * kTile * a.r2ld + c0;
                 R.ldc = a.r2ld;
                 R.rows = a.r2rows - ti * kTile;
+            } else {
+                const int64_t u = t - tiles_d - (n1 + n2) * ntd;
+                ti = u / ntd;
+                R.cj = u % ntd;
+                R.C = a.xinv + ti * kTile * a.xld + c1;
+                R.A = a.xinv + ti * kTile * a.xld + c0;
+                R.ldc = a.xld;
+                R.rows = m - ti * kTile;
+                R.fresh = ti == p;
             }
             if (R.rows > kTile) R.rows = kTile;
             R.cols = (m - c1) - R.cj * kTile;
@@ -403,7 +431,8 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
             return R;
         };
         constexpr int U = kTile * kTile / NT;
-        T va[U], vb[U];
+        const int cx = tid & 15, cy = tid >> 4;
+        T va[U], vb[U], vc[2][2];
         auto fetch = [&](const TileRef& R) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -411,6 +440,15 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                 va[u] = (r < R.rows && k < w) ? ldcg(R.A + (int64_t)r * R.ldc + k) : T(0);
                 vb[u] = (r < R.cols && k < w) ? ldcg(Bpan + (R.cj * kTile + r) * a.ldd + k) : T(0);
             }
+#pragma unroll
+            for (int i2 = 0; i2 < 2; ++i2)
+#pragma unroll
+                for (int j2 = 0; j2 < 2; ++j2) {
+                    const int r = cy + 16 * i2, c = cx + 16 * j2;
+                    vc[i2][j2] = (!R.fresh && r < R.rows && c < R.cols)
+                                     ? ldcg(R.C + (int64_t)r * R.ldc + R.cj * kTile + c)
+                                     : T(0);
+                }
         };
         int64_t t = t0 + wk;
         TileRef cur;
@@ -427,31 +465,31 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                 As[e / kTile][e % kTile] = va[u];
                 Bs[e / kTile][e % kTile] = vb[u];
             }
+            T acc[2][2];
+#pragma unroll
+            for (int i2 = 0; i2 < 2; ++i2)
+#pragma unroll
+                for (int j2 = 0; j2 < 2; ++j2) acc[i2][j2] = vc[i2][j2];
             __syncthreads();
             const TileRef now = cur;
             if (t + nwk < total) {  // next tile's operands in flight during this tile's FMAs
                 cur = tile_ref(t + nwk);
                 fetch(cur);
             }
-            const int cx = tid & 15, cy = tid >> 4;
-            T acc[2][2] = {{T(0), T(0)}, {T(0), T(0)}};
             for (int k = 0; k < w; ++k) {
                 const T a0 = As[cy][k], a1 = As[cy + 16][k];
                 const T b0 = Bs[cx][k], b1 = Bs[cx + 16][k];
-                acc[0][0] = fma(a0, b0, acc[0][0]);
-                acc[0][1] = fma(a0, b1, acc[0][1]);
-                acc[1][0] = fma(a1, b0, acc[1][0]);
-                acc[1][1] = fma(a1, b1, acc[1][1]);
+                acc[0][0] = fma(-a0, b0, acc[0][0]);
+                acc[0][1] = fma(-a0, b1, acc[0][1]);
+                acc[1][0] = fma(-a1, b0, acc[1][0]);
+                acc[1][1] = fma(-a1, b1, acc[1][1]);
             }
 #pragma unroll
             for (int i2 = 0; i2 < 2; ++i2)
 #pragma unroll
                 for (int j2 = 0; j2 < 2; ++j2) {
                     const int r = cy + 16 * i2, c = cx + 16 * j2;
-                    if (r < now.rows && c < now.cols) {
-                        T* cp = now.C + (int64_t)r * now.ldc + now.cj * kTile + c;
-                        *cp = ldcg(cp) - acc[i2][j2];
-                    }
+                    if (r < now.rows && c < now.cols) now.C[(int64_t)r * now.ldc + now.cj * kTile + c] = acc[i2][j2];
                 }
         }
         if (!group_barrier(barC, G - kW0, epC, a.status, &S.flag)) return;
@@ -465,7 +503,7 @@ int g_panel_grid[64] = {};
 template <typename T>
 cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, RowSet<T> r2, T* tinv,
                                     unsigned* bar, int32_t* status, int32_t* info, int64_t info_row0,
-                                    cudaStream_t s) {
+                                    cudaStream_t s, T* xinv) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -491,6 +529,8 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
     a.r2 = r2.p;
     a.r2rows = r2.p ? r2.rows : 0;
     a.r2ld = r2.ld;
+    a.xinv = xinv;
+    a.xld = m;
     a.scratch = tinv;
     a.info = info;
     a.row0 = info_row0;
@@ -502,15 +542,18 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
     prof_before(s);
     e = cudaLaunchCooperativeKernel((const void*)k_factor_panel<T>, dim3(G), dim3(NT), args, 0, s);
     // useful flops: Cholesky of the m x m block + TRSM of the rows below it
+    // (+ the triangular inverse)
     const double md = (double)m;
-    prof_after(SGB_KCLASS_PANEL, s, md * md * md / 3.0 + (double)(a.r1rows + a.r2rows) * md * md);
+    prof_after(SGB_KCLASS_PANEL, s,
+               md * md * md / 3.0 * (xinv ? 2.0 : 1.0) + (double)(a.r1rows + a.r2rows) * md * md);
     return e;
 }
 
 template cudaError_t factor_panel_persistent<double>(double*, int64_t, int64_t, RowSet<double>, RowSet<double>,
-                                                     double*, unsigned*, int32_t*, int32_t*, int64_t,
-                                                     cudaStream_t);
+                                                     double*, unsigned*, int32_t*, int32_t*, int64_t, cudaStream_t,
+                                                     double*);
 template cudaError_t factor_panel_persistent<float>(float*, int64_t, int64_t, RowSet<float>, RowSet<float>,
-                                                    float*, unsigned*, int32_t*, int32_t*, int64_t, cudaStream_t);
+                                                    float*, unsigned*, int32_t*, int32_t*, int64_t, cudaStream_t,
+                                                    float*);
 
 }  // namespace sgb
