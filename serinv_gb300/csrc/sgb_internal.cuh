@@ -103,7 +103,8 @@ template <typename T>
 using GemmFn = cudaError_t (*)(void* ctx, GemmProb<T>* probs, int np, cudaStream_t s);
 
 // The same column-block factorization as one cooperative persistent launch
-// (sgb_panel.cu).  `bar` is 16 unsigned words of scratch; `status` receives
+// (sgb_panel.cu).  `tinv` is 7 * kTile * kTile + 6 * kTile elements of
+// scratch, `bar` 16 unsigned words; `status` receives
 // SGB_ERR_TIMEOUT if a grid barrier gives up.  With `xinv` (m x m,
 // row-major, ld m) the launch also writes L^{-T} there: its upper block
 // triangle including the diagonal tiles (zeros below the diagonal inside

@@ -10,32 +10,38 @@
 //
 //   CTA 0        factorizer: diagonal tile p as L = M D^{1/2} (the pivot
 //                pipeline of factor_tile_m), whose warp 4 publishes the
-//                columns of M and the pivots d as they are produced
+//                columns of M, d and d^{-1/2} as they are produced
 //                (counter of published columns), then counter F at the end
-//                of the tile; waits for the helpers (counter H2) before
-//                tile p+1;
+//                of the tile; tile p+1 arrives by value from the helpers;
 //   CTAs 1..kNH  helpers: the rows of tile-row p+1 in column block p by
 //                unit-triangular substitution (Y M^T = B, X = Y D^{-1/2}),
-//                following the published columns (counter H1), then their
-//                rows of the update of tile (p+1, p+1) (counter H2); after
-//                barrier B they apply column block p to their rows of
-//                tile-row p+2 (tiles (p+2, p+1) and (p+2, p+2)), so
-//                nothing the next step needs waits for the bulk update;
+//                following the published columns, handed to each other by
+//                value; then their rows of the update of tile (p+1, p+1),
+//                handed to the factorizer by value; after barrier B they
+//                apply column block p to their rows of tile-row p+2 (tiles
+//                (p+2, p+1) and (p+2, p+2)), so nothing the next step needs
+//                waits for the bulk update;
 //   CTA kNH+1    L writer: from M_p, d_p the tile's L into the matrix
 //                (counter I);
-//   CTAs kNH+2.. workers: the other rows below tile p, by the same
-//                substitution following the published columns, barrier B
-//                (with the helpers), the rank-32 update of the rest of the
-//                trailing panel (the next tile's operands loaded during the
-//                current tile's FMAs), barrier C (workers only).
+//   CTAs kNH+2.. workers: the other rows below tile p (and, with xinv, the
+//                rows of L^{-T}), by the same substitution following the
+//                published columns, barrier B (with the helpers), the
+//                rank-32 update of the rest of the trailing panel (the next
+//                tile's operands and C loaded during the current tile's
+//                FMAs), barrier C (workers only).
 //
-// M and d alternate between two buffers by the parity of p; the factorizer
-// waits for the L writer before overwriting a buffer.  Every wait is a
-// bounded poll of a word in global memory: one that does not complete
-// within the limit sets the status word to SGB_ERR_TIMEOUT and the CTA
-// leaves (the cooperative launch guarantees that all CTAs are resident, so
-// no wait depends on an unscheduled CTA).  Data produced by other CTAs is
-// read with ld.global.cg (L2), never from a possibly stale L1 line.
+// M, d and d^{-1/2} rotate through three buffers; the factorizer waits for
+// the L writer before overwriting one.  The two hand-offs on the chain from
+// one diagonal tile to the next go by value through staging buffers (a
+// sentinel NaN until the producer stores the value, see Staged<T>), so no
+// fence or counter sits between producer and consumer; the factorizer
+// resets each staging buffer once its consumers are provably done.  Every
+// other wait is a bounded poll of a word in global memory: one that does
+// not complete within the limit sets the status word to SGB_ERR_TIMEOUT
+// and the CTA leaves (the cooperative launch guarantees that all CTAs are
+// resident, so no wait depends on an unscheduled CTA).  Data produced by
+// other CTAs is read with ld.global.cg (L2) or relaxed GPU-scope loads,
+// never from a possibly stale L1 line.
 #include <math.h>
 
 #include "sgb_internal.cuh"
@@ -62,11 +68,12 @@ struct PanelArgs {
     int64_t r2rows, r2ld;
     T* xinv;  // m x m, row-major (ld xld): L^{-T} out, or null
     int64_t xld;
-    T* scratch;  // [2][32][32] (unused), [2][32][32] M^T by column, [2][32] d
+    T* scratch;  // [3][32][32] M^T by column, [3][32] d, [3][32] d^{-1/2},
+                 // [2][32][32] staged diagonal tiles, [2][32][32] staged tile-rows
     int32_t* info;
     int64_t row0;
-    unsigned* bar;    // [0] F, [1] I, [2] H1, [3] H2, [4] barrier B, [6] barrier C,
-                      // [8] columns of M published; zero at launch
+    unsigned* bar;    // [0] F, [1] I, [4] barrier B, [6] barrier C, [8] columns of M
+                      // published; zero at launch
     int32_t* status;  // SGB_ERR_TIMEOUT on a stuck wait
 };
 
@@ -113,8 +120,8 @@ __device__ __forceinline__ bool group_barrier(unsigned* cnt, unsigned nblocks, u
     return *sflag != 0;
 }
 
-// Wait until *ctr >= target; false (on every thread) on a timeout or an
-// error raised elsewhere.
+// Wait until *ctr >= target (tight poll: only a few CTAs wait here); false
+// (on every thread) on a timeout or an error raised elsewhere.
 __device__ __forceinline__ bool wait_count(const unsigned* ctr, unsigned target, int32_t* status, int* sflag) {
     if (threadIdx.x == 0) {
         long long spins = 0;
@@ -125,7 +132,6 @@ __device__ __forceinline__ bool wait_count(const unsigned* ctr, unsigned target,
                 atomicExch(status, SGB_ERR_TIMEOUT);
                 break;
             }
-            __nanosleep(32);
         }
         __threadfence();
         *sflag = ok;
@@ -134,11 +140,23 @@ __device__ __forceinline__ bool wait_count(const unsigned* ctr, unsigned target,
     return *sflag != 0;
 }
 
-// Publish: make this CTA's global writes visible, then count on ctr.
-__device__ __forceinline__ void signal(unsigned* ctr) {
-    __threadfence();
+// CTA-uniform check of the status word (also a CTA barrier).
+__device__ __forceinline__ bool cta_ok(const int32_t* status, int* sflag) {
     __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(ctr, 1u);
+    if (threadIdx.x == 0) *sflag = !status_bad(status);
+    __syncthreads();
+    return *sflag != 0;
+}
+
+// Publish: make this CTA's global writes visible, then count on ctr (the
+// barrier orders the CTA's writes before thread 0's fence, which is
+// cumulative).
+__device__ __forceinline__ void signal(unsigned* ctr) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr, 1u);
+    }
 }
 
 // Row r of the unified row space [D rows c1..m) ++ r1 rows ++ r2 rows.
@@ -154,17 +172,21 @@ __device__ __forceinline__ T* row_ptr(const PanelArgs<T>& a, int64_t c1, int64_t
 // One row per warp: row <- row * L^{-T} over the w columns of the row
 // pointer, with L = M diag(d)^{1/2}: Y M^T = row by substitution (lane =
 // column; one shuffle and one FMA per column), X = Y diag(d)^{-1/2}.  The
-// columns of M (transposed in mt) and the pivots dv are consumed as the
+// columns of M (transposed in mt) and d^{-1/2} (rv) are consumed as the
 // factorizer publishes them: column k once *colcount >= col_base + k + 1
-// (bounded wait), all available columns loaded at once.  With unit >= 0
+// (bounded wait; `sleep` backs off between polls), all available columns
+// loaded at once.  With stage_row the result also goes to that staging row
+// (hand-off by value).  With unit >= 0
 // the row is the unit vector e_unit instead of the stored values (a row of
 // the identity, whose solve is a row of L^{-T}).  Returns false on a
 // timeout or an error raised elsewhere.
 template <typename T>
-__device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T* dv, const unsigned* colcount,
-                                              unsigned col_base, int32_t* status, int unit = -1) {
+__device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T* rv, const unsigned* colcount,
+                                              unsigned col_base, int32_t* status, bool sleep, int unit = -1,
+                                              T* stage_row = nullptr) {
     const int tx = threadIdx.x & 31;
     T y = tx < w ? (unit >= 0 ? T(tx == unit ? 1 : 0) : ldcg(rp + tx)) : T(0);
+    T r = T(0);
     int k = 0;
     long long spins = 0;
     while (k < w) {
@@ -179,7 +201,7 @@ __device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T
                     avail = -1;
                     break;
                 }
-                __nanosleep(32);
+                if (sleep) __nanosleep(32);
             }
         }
         avail = __shfl_sync(0xffffffffu, avail, 0);
@@ -190,6 +212,7 @@ __device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T
             T mk[kTile];
 #pragma unroll
             for (int u = 0; u < kTile; ++u) mk[u] = u < nb ? ldcg(mt + (k + u) * kTile + tx) : T(0);
+            if (tx >= k && tx < k + nb) r = ldcg(rv + tx);
 #pragma unroll
             for (int u = 0; u < kTile; ++u) {
                 if (u < nb) {
@@ -200,7 +223,11 @@ __device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T
             k += nb;
         }
     }
-    if (tx < w) rp[tx] = y * rsq<T>(ldcg(dv + tx));
+    if (tx < w) {
+        const T x = y * r;
+        rp[tx] = x;
+        if (stage_row != nullptr) stage_put(stage_row + tx, x);
+    }
     return true;
 }
 
@@ -248,24 +275,34 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
     const int tx = tid & 31, ty = tid >> 5;
     unsigned* F = a.bar + 0;
     unsigned* I = a.bar + 1;
-    unsigned* H1 = a.bar + 2;
-    unsigned* H2 = a.bar + 3;
     unsigned* barB = a.bar + 4;
     unsigned* barC = a.bar + 6;
     unsigned* CC = a.bar + 8;
-    T* Mg = a.scratch + 2 * kTile * kTile;  // [2][32*32], column k of M at [k][0..31]
-    T* dg = a.scratch + 4 * kTile * kTile;  // [2][32]
+    T* Mg = a.scratch;                      // [3][32*32], column k of M at [k][0..31]
+    T* dg = a.scratch + 3 * kTile * kTile;  // [3][32] d
+    T* rg = dg + 3 * kTile;                 // [3][32] d^{-1/2}
+    T* stT = rg + 3 * kTile;                // [2][32*32] tile (p, p) after its last update, by value
+    T* stL = stT + 2 * kTile * kTile;       // [2][32*32] tile-row p+1 in column block p, by value
     auto tile_w = [&](int64_t p) -> int { return (int)((m - p * kTile) < kTile ? (m - p * kTile) : kTile); };
 
     if (cta == 0) {
         // ---------------- factorizer
+        // staging buffers to the sentinel before the first column is
+        // published (every later hand-off is ordered after it)
+        for (int e = tid; e < 4 * kTile * kTile; e += NT) stage_clear(stT + e);
+        __syncthreads();
         for (int64_t p = 0; p < nt; ++p) {
             const int64_t c0 = p * kTile;
             const int w = tile_w(p);
-            if (p >= 1 && !wait_count(H2, (unsigned)(kNH * p), a.status, &S.flag)) return;
-            if (p >= 2 && !wait_count(I, (unsigned)(p - 1), a.status, &S.flag)) return;
-            factor_tile_m<T>(S, a.diag + c0 * a.ldd + c0, a.ldd, w, a.info, a.row0 + c0, Mg + (p & 1) * kTile * kTile,
-                             dg + (p & 1) * kTile, CC, (unsigned)(p * kTile));
+            if (p >= 3 && !wait_count(I, (unsigned)(p - 2), a.status, &S.flag)) return;  // buffer p % 3 free
+            const int buf = (int)(p % 3);
+            // tile p >= 1 arrives by value from the helpers (their update
+            // with column block p-1); tile-row staging p-1 is then free
+            factor_tile_m<T>(S, a.diag + c0 * a.ldd + c0, a.ldd, w, a.info, a.row0 + c0, Mg + buf * kTile * kTile,
+                             dg + buf * kTile, rg + buf * kTile, CC, (unsigned)(p * kTile),
+                             p >= 1 ? stT + (p & 1) * kTile * kTile : nullptr,
+                             p >= 1 ? stL + ((p - 1) & 1) * kTile * kTile : nullptr, a.status);
+            if (!cta_ok(a.status, &S.flag)) return;
             signal(F);
         }
         return;
@@ -276,13 +313,17 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
             const int64_t c0 = p * kTile;
             const int w = tile_w(p);
             if (!wait_count(F, (unsigned)(p + 1), a.status, &S.flag)) return;
+            const int buf = (int)(p % 3);
             {
-                const T* mt = Mg + (p & 1) * kTile * kTile;
+                const T* mt = Mg + buf * kTile * kTile;
                 for (int e = tid; e < kTile * kTile; e += NT) S.x[e % kTile][e / kTile] = ldcg(mt + e);
             }
-            if (tid < kTile) S.yv[tid] = ldcg(dg + (p & 1) * kTile + tid);
+            if (tid < kTile) {
+                S.yv[tid] = ldcg(dg + buf * kTile + tid);
+                S.tmp[0][tid] = ldcg(rg + buf * kTile + tid);
+            }
             __syncthreads();
-            tile_l_from_m<T>(S.x, S.yv, a.diag + c0 * a.ldd + c0, a.ldd, w, (int)(m - c0 - w));
+            tile_l_from_m<T>(S.x, S.yv, &S.tmp[0][0], a.diag + c0 * a.ldd + c0, a.ldd, w, (int)(m - c0 - w));
             signal(I);
         }
         return;
@@ -299,32 +340,53 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         const int64_t c2 = c1 + w2;
         const bool has_next2 = c2 < m;
         const int w3 = has_next2 ? tile_w(p + 2) : 0;
-        const T* Mp = Mg + (p & 1) * kTile * kTile;
-        const T* dp = dg + (p & 1) * kTile;
+        const T* Mp = Mg + (p % 3) * kTile * kTile;
+        const T* rp3 = rg + (p % 3) * kTile;
 
         if (helper) {
             if (!has_next) break;
             // rows of tile-row p+1 in column block p (Y M^T = B, X = Y D^{-1/2}),
             // column by column as the factorizer publishes M; a timeout sets
             // the status word, which the wait below sees
+            T* sL = stL + (p & 1) * kTile * kTile;
             if (ty < kHelpRows) {
                 const int r = h * kHelpRows + ty;
                 if (r < w2)
-                    trsm_row_pipe<T>(a.diag + (c1 + r) * a.ldd + c0, w, Mp, dp, CC, (unsigned)(p * kTile), a.status);
+                    trsm_row_pipe<T>(a.diag + (c1 + r) * a.ldd + c0, w, Mp, rp3, CC, (unsigned)(p * kTile), a.status,
+                                     false, -1, sL + r * kTile);
             }
-            signal(H1);
-            if (!wait_count(H1, (unsigned)(kNH * (p + 1)), a.status, &S.flag)) return;
-            // their rows of the update of tile (p+1, p+1) with column block p
-            load_block<T>(S.tmp, a.diag + c1 * a.ldd + c0, a.ldd, w2, w);
-            __syncthreads();
-            if (ty < kHelpRows) {
-                const int rr = h * kHelpRows + ty, c = tx;
-                if (rr < w2 && c <= rr) {
-                    T* cp = a.diag + (c1 + rr) * a.ldd + c1 + c;
-                    *cp = ldcg(cp) - dot32<T>(&S.tmp[rr][0], &S.tmp[c][0], w);
+            // The staging row buffer was reset during tile p-1, ordered
+            // before tile p's columns: acquire one of those (done already
+            // where this CTA had rows to solve) before any thread polls it.
+            if (!wait_count(CC, (unsigned)(p * kTile + 1), a.status, &S.flag)) return;
+            // this thread's element of tile (p+1, p+1) (last written by this CTA)
+            const int rr1 = h * kHelpRows + ty, cc1 = tx;
+            const bool own1 = ty < kHelpRows && rr1 < w2 && cc1 <= rr1;
+            const T cold = own1 ? ldcg(a.diag + (c1 + rr1) * a.ldd + c1 + cc1) : T(0);
+            // all of tile-row p+1 by value from the helpers, then their rows
+            // of the update of tile (p+1, p+1), handed to the factorizer by value
+            {
+                constexpr int U = kTile * kTile / NT;
+                const T* sp[U];
+                bool want[U];
+                T v[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int e = tid + u * NT;
+                    sp[u] = sL + e;
+                    want[u] = e / kTile < w2 && e % kTile < w;
+                }
+                if (!stage_take<T, U>(sp, want, v, kBarrierSpin, a.status)) atomicExch(a.status, SGB_ERR_TIMEOUT);
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int e = tid + u * NT;
+                    S.tmp[e / kTile][e % kTile] = want[u] ? v[u] : T(0);
                 }
             }
-            signal(H2);
+            if (!cta_ok(a.status, &S.flag)) return;
+            if (own1)
+                stage_put(stT + ((p + 1) & 1) * kTile * kTile + rr1 * kTile + cc1,
+                          cold - dot32<T>(&S.tmp[rr1][0], &S.tmp[cc1][0], w));
             // after the bulk TRSM: column block p applied to their rows of tile-row p+2
             if (!group_barrier(barB, G - 2, epB, a.status, &S.flag)) return;
             if (has_next2) {
@@ -365,7 +427,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                 rp = a.xinv + xr * a.xld + c0;
                 if (xr >= c0) unit = (int)(xr - c0);
             }
-            if (!trsm_row_pipe<T>(rp, w, Mp, dp, CC, (unsigned)(p * kTile), a.status, unit)) break;
+            if (!trsm_row_pipe<T>(rp, w, Mp, rp3, CC, (unsigned)(p * kTile), a.status, true, unit)) break;
         }
         if (!has_next) break;
         if (!group_barrier(barB, G - 2, epB, a.status, &S.flag)) return;

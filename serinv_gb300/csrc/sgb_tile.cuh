@@ -43,6 +43,7 @@ struct Smem {
     unsigned short tri[kTile * (kTile + 1) / 2];  // (row << 8) | col of the lower triangle, row-major
     int fail;
     int flag;
+    int pub;  // factor_tile_m: columns the companion has completed
 };
 
 // Recursive-doubling inverse of the (identity padded) lower tile s into x.
@@ -133,6 +134,88 @@ __device__ __forceinline__ float rcp_pivot(float d) { return 1.0f / d; }
 __device__ __forceinline__ void nbar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 __device__ __forceinline__ void nbar_arrive(int id, int n) {
     asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+// Hand-off by value: a staging element holds a signaling NaN whose payload
+// no arithmetic produces (results are canonical quiet NaNs) until its
+// producer stores the real value with a relaxed GPU-scope store; the
+// consumer polls the element itself, so no fence and no counter sit
+// between them.  Single-copy atomicity of aligned 4- and 8-byte accesses
+// makes the poll see either the sentinel or the whole value.
+template <typename T>
+struct Staged;
+template <>
+struct Staged<double> {
+    static constexpr unsigned long long kSentinel = 0x7FF0DEADBEEF5EB1ull;
+    static __device__ __forceinline__ unsigned long long ld(const double* p) {
+        unsigned long long v;
+        asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+        return v;
+    }
+    static __device__ __forceinline__ void st(double* p, unsigned long long v) {
+        asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    }
+    static __device__ __forceinline__ double val(unsigned long long v) { return __longlong_as_double((long long)v); }
+    static __device__ __forceinline__ unsigned long long bits(double x) {
+        return (unsigned long long)__double_as_longlong(x);
+    }
+};
+template <>
+struct Staged<float> {
+    static constexpr unsigned kSentinel = 0x7F8DEAD5u;
+    static __device__ __forceinline__ unsigned ld(const float* p) {
+        unsigned v;
+        asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+        return v;
+    }
+    static __device__ __forceinline__ void st(float* p, unsigned v) {
+        asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+    }
+    static __device__ __forceinline__ float val(unsigned v) { return __uint_as_float(v); }
+    static __device__ __forceinline__ unsigned bits(float x) { return __float_as_uint(x); }
+};
+
+template <typename T>
+__device__ __forceinline__ void stage_put(T* p, T x) {
+    Staged<T>::st(p, Staged<T>::bits(x));
+}
+template <typename T>
+__device__ __forceinline__ void stage_clear(T* p) {
+    Staged<T>::st(p, Staged<T>::kSentinel);
+}
+// Poll up to U elements p[u] (those with want[u]) until each holds a value;
+// the loads of one round are all issued before any is tested.  Bounded:
+// false after `limit` rounds, or once *status is non-zero (checked every
+// 64 rounds); missing values then read as NaN.
+template <typename T, int U>
+__device__ __forceinline__ bool stage_take(const T* const (&p)[U], const bool (&want)[U], T (&out)[U],
+                                           long long limit, const int32_t* status) {
+    bool have[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) have[u] = !want[u];
+    for (long long i = 0; i < limit; ++i) {
+        decltype(Staged<T>::ld(p[0])) raw[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) raw[u] = have[u] ? Staged<T>::kSentinel : Staged<T>::ld(p[u]);
+        bool all = true;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (!have[u] && raw[u] != Staged<T>::kSentinel) {
+                out[u] = Staged<T>::val(raw[u]);
+                have[u] = true;
+            }
+            all = all && have[u];
+        }
+        if (all) return true;
+        if ((i & 63) == 63 && status != nullptr && *(const volatile int32_t*)status != 0) break;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+        if (!have[u]) out[u] = T(NAN);
+    return false;
 }
 
 // Unit-lower inverse Z = M^{-1} from its 8 x 8 diagonal blocks (already in
@@ -318,38 +401,68 @@ __device__ void factor_tile(Smem<T>& S, T* tile, int64_t ld, int nb, int zero_ri
 //   pivot warp (q_{j+2}, e_{j+2}) -- four FP64 instructions per column;
 // * warps 2, 3, 6, 7 (quarters 2 and 3) apply column k to the strict lower
 //   part of columns k+2.. (the companion keeps the diagonal), then UPD;
-// * with `mt` set, warp 4 publishes the factor column by column: column k
-//   of M to mt[k][0..31] (transposed, so a column is one coalesced row) and
-//   d_k to dv[k]; every eight columns (every second one from column 24, and
-//   after the last) it makes them visible at GPU scope and sets
-//   *colcount = col_base + k + 1, so other CTAs can consume the columns as
-//   they appear.  It takes part in READY/UPD either way (no FP64 work).
+// * with `mt` set, warp 4 publishes the factor outside the pipeline: the
+//   companion counts its finished columns in S.pub (release at CTA scope);
+//   the publisher takes every column finished since its last pass --
+//   column k of M to mt[k][0..31] (transposed, so a column is one coalesced
+//   row), d_k to dv[k] and d_k^{-1/2} to rv[k] -- makes them visible at GPU
+//   scope and sets *colcount = col_base + (columns published), so other
+//   CTAs consume the columns as they appear.  Its GPU-scope fences never
+//   hold up the pivot pipeline; the chunks grow when a fence is slow.
+//
+// With `staged` the tile's lower part comes from that 32 x 32 staging
+// buffer (ld 32) instead of `tile`, each element taken as its producer
+// stores it and reset to the sentinel; `clear` (32 x 32) is reset to the
+// sentinel; a poll that gives up sets *status = SGB_ERR_TIMEOUT.
 //
 // Pivot <-> companion hand-offs use named barriers PQ (ids 5, 6) and QP
-// (7, 8), READY/UPD ids 1-4; every pair alternates between two ids so that
-// no side can run two generations ahead (the arrival sequence was checked
-// on a CPU model for nb = 1..32).
+// (7, 8), READY/UPD ids 1-4 (companion + workers); every pair alternates
+// between two ids so that no side can run two generations ahead (the
+// arrival sequence was checked on a CPU model for nb = 1..32).
 template <typename T>
 __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int32_t* info, int64_t row0,
-                              T* mt = nullptr, T* dv = nullptr, unsigned* colcount = nullptr,
-                              unsigned col_base = 0) {
+                              T* mt = nullptr, T* dv = nullptr, T* rv = nullptr, unsigned* colcount = nullptr,
+                              unsigned col_base = 0, T* staged = nullptr, T* clear = nullptr,
+                              int32_t* status = nullptr) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr int kCons = 32 * 6;  // companion + four workers + publisher
+    constexpr int kCons = 32 * 5;  // companion + four workers
     constexpr int kPair = 64;
     T* iv = &S.tmp[0][0];  // 1/d_j
     T* qv = &S.tmp[1][0];  // a'_{j,j-1}^2
     T* ev = &S.tmp[2][0];  // diagonal of column j through column j-2
-    for (int e = tid; e < kTile * kTile; e += kTileThreads) {
-        const int r = e / kTile, c = e % kTile;
+    constexpr int U = kTile * kTile / kTileThreads;
+    bool timed_out = false;
+    T sv[U];
+    if (staged != nullptr) {  // lower part of the tile as its producers store it
+        const T* sp[U];
+        bool want[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int e = tid + u * kTileThreads, r = e / kTile, c = e % kTile;
+            sp[u] = staged + e;
+            want[u] = r < nb && c <= r;
+        }
+        timed_out = !stage_take<T, U>(sp, want, sv, 1ll << 22, status);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (want[u]) stage_clear(staged + tid + u * kTileThreads);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int e = tid + u * kTileThreads, r = e / kTile, c = e % kTile;
         T v = T(0);
-        if (r < nb && c <= r) v = __ldcg(tile + (int64_t)r * ld + c);
+        if (r < nb && c <= r) v = staged != nullptr ? sv[u] : __ldcg(tile + (int64_t)r * ld + c);
         else if (r >= nb && r == c) v = T(1);
         S.s[r][c] = v;
         S.x[r][c] = T(0);
         if (c < r) S.tri[r * (r - 1) / 2 + c] = (unsigned short)((r << 8) | c);  // strict lower, row-major
     }
     if (tid < kTile) S.yv[tid] = T(1);
-    if (tid == 0) S.fail = 0;
+    if (tid == 0) {
+        S.fail = 0;
+        S.pub = 0;
+    }
+    if (timed_out && status != nullptr) atomicExch(status, SGB_ERR_TIMEOUT);
     __syncthreads();
     if (warp == 0) {
         T d = S.s[0][0];
@@ -386,6 +499,11 @@ __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int
             const T mcol = col * inv;
             if (lane >= j) S.s[lane][j] = col;
             if (lane > j) S.x[lane][j] = mcol;
+            if (mt != nullptr) {  // column j (and d_j, seen through PQ(j)) to the publisher
+                __syncwarp();
+                if (lane == 0) asm volatile("st.release.cta.shared.u32 [%0], %1;" ::"r"(smem_u32(&S.pub)), "r"(j + 1)
+                                            : "memory");
+            }
             nbar_arrive(1 + (j & 1), kCons);  // READY(j)
             if (j >= 1) nbar_sync(3 + ((j - 1) & 1), kCons);  // UPD(j-1)
             if (j + 1 < nb) {
@@ -403,21 +521,34 @@ __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int
             }
         }
     } else if (warp == 4) {
-        for (int k = 0; k < nb; ++k) {
-            nbar_sync(1 + (k & 1), kCons);  // READY(k)
-            if (mt != nullptr) {
-                mt[k * kTile + lane] = S.x[lane][k];
-                if (lane == 0) dv[k] = S.yv[k];
-            }
-            if (k + 1 < nb) nbar_arrive(3 + (k & 1), kCons);  // UPD(k)
-            // publish every eighth column, every second one near the end
-            if (mt != nullptr && ((k & 7) == 7 || (k >= 24 && (k & 1)) || k == nb - 1)) {
+        if (mt != nullptr) {
+            int done = 0;
+            long long spins = 0;
+            while (done < nb) {
+                int avail = 0;
+                for (;;) {  // bounded: the companion finishes every column in any case
+                    asm volatile("ld.acquire.cta.shared.u32 %0, [%1];" : "=r"(avail) : "r"(smem_u32(&S.pub)) : "memory");
+                    if (avail > done || ++spins > (1ll << 26)) break;
+                }
+                if (avail <= done) break;  // the waits of the consumers time out and report it
+                for (int k = done; k < avail; ++k) mt[k * kTile + lane] = S.x[lane][k];
+                if (lane >= done && lane < avail) {
+                    const T d = S.yv[lane];
+                    dv[lane] = d;
+                    rv[lane] = rsq<T>(d);
+                }
                 __threadfence();
                 __syncwarp();
-                if (lane == 0) atomicExch(colcount, col_base + (unsigned)k + 1u);
+                if (lane == 0) atomicExch(colcount, col_base + (unsigned)avail);
+                done = avail;
             }
         }
-    } else if (warp != 5) {
+    } else if (warp == 5) {
+        // every consumer of `clear` is done with it (they all produced the
+        // staged values taken above)
+        if (clear != nullptr)
+            for (int e = lane; e < kTile * kTile; e += 32) stage_clear(clear + e);
+    } else {
         const int wid = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;  // 0..127
         for (int k = 0; k < nb; ++k) {
             nbar_sync(1 + (k & 1), kCons);  // READY(k)
@@ -435,17 +566,18 @@ __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int
     if (tid == 0 && S.fail != 0 && info != nullptr) atomicCAS(info, 0, (int32_t)(row0 + S.fail));
 }
 
-// The tile's L = M diag(d)^{1/2} from M (strict lower, in m) and the
-// pivots d (in dv) into `tile`, the upper part and the zero_right columns
-// to the right of the tile set to zero.
+// The tile's L = M diag(d)^{1/2} from M (strict lower, in m), the pivots d
+// (in dv) and d^{-1/2} (in rv) into `tile`, the upper part and the
+// zero_right columns to the right of the tile set to zero.
 template <typename T>
-__device__ void tile_l_from_m(T (*m)[kTile + 1], const T* dv, T* tile, int64_t ld, int nb, int zero_right) {
+__device__ void tile_l_from_m(T (*m)[kTile + 1], const T* dv, const T* rv, T* tile, int64_t ld, int nb,
+                              int zero_right) {
     const int tid = threadIdx.x;
     for (int e = tid; e < nb * nb; e += kTileThreads) {
         const int r = e / nb, c = e - (e / nb) * nb;
         T lv = T(0);
         if (c <= r) {
-            const T sq = dv[c] * rsq<T>(dv[c]);  // sqrt(d_c)
+            const T sq = dv[c] * rv[c];  // sqrt(d_c)
             lv = (c < r) ? m[r][c] * sq : sq;
         }
         tile[(int64_t)r * ld + c] = lv;
