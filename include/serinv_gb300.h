@@ -217,6 +217,11 @@ long long sgb_launch_count(void);
 /* Enable (1) or disable (0) per-launch CUDA-event timing; clears records. */
 int sgb_profile_enable(int on);
 
+/* Time only the kernel classes in `mask` (bit SGB_KCLASS_*); 0 disables.
+ * Events bracket the timed launches only, so the others keep overlapping
+ * their neighbours (programmatic dependent launch).  Clears records. */
+int sgb_profile_enable_classes(unsigned mask);
+
 /* Totals over the recorded launches of one class: launch count, device
  * milliseconds between the events bracketing each launch, and algorithmic
  * flops (useful multiply-adds x 2).  Synchronises on the recorded events. */

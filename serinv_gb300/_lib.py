@@ -99,6 +99,7 @@ _SIGNATURES = {
     "sgb_batch_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "sgb_launch_count": (ctypes.c_longlong, []),
     "sgb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
+    "sgb_profile_enable_classes": (ctypes.c_int, [ctypes.c_uint]),
     "sgb_profile_read": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
@@ -142,8 +143,12 @@ def launch_count() -> int:
     return int(load().sgb_launch_count())
 
 
-def profile_enable(on: bool) -> None:
-    load().sgb_profile_enable(1 if on else 0)
+def profile_enable(on: bool, classes=None) -> None:
+    """Per-launch event timing: off, all kernel classes, or only `classes` (names of KCLASS)."""
+    if classes is None or not on:
+        load().sgb_profile_enable(1 if on else 0)
+    else:
+        load().sgb_profile_enable_classes(sum(1 << KCLASS[c] for c in classes))
 
 
 def profile_read() -> dict:

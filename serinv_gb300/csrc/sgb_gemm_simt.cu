@@ -183,7 +183,7 @@ cudaError_t gemm_simt(GemmProb<T>* probs, int np, cudaStream_t s) {
     L.total_tiles = (int32_t)total;
     double fl = 0.0;
     for (int i = 0; i < L.np; ++i) fl += useful_flops<T>(L.p[i]);
-    prof_before(s);
+    prof_before(s, SGB_KCLASS_GEMM);
     k_gemm_simt<T><<<(unsigned)total, NT, 0, s>>>(L);
     prof_after(SGB_KCLASS_GEMM, s, fl);
     return cudaGetLastError();

@@ -143,10 +143,21 @@ __device__ __forceinline__ void digits(double x, int Erow, int (&d)[S]) {
 // of every element are written in the chunk layout the MMA descriptors
 // read -- padding rows and the K padding of each term as zeros, so the
 // buffers need no clearing beforehand.
+// Programmatic dependent launch: the kernels of a product are launched
+// with programmatic stream serialization, so a launch may start while its
+// predecessor in the stream drains.  Every kernel waits for the
+// predecessor's completion (and memory) before its first global access,
+// then lets its own successor start launching.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <int S>
 __global__ void __launch_bounds__(kSplitThreads) k_split(const __grid_constant__ SplitLaunch L) {
     __shared__ double t[kSplitRows][kSplitLd];
     __shared__ int ex[kSplitRows];
+    pdl_enter();
     const SplitJob& J = L.j[find_job(L, blockIdx.x)];
     const int local = blockIdx.x - J.strip_begin;
     const int inst = local / J.strips;
@@ -480,6 +491,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    pdl_enter();
 
     const int nkb_all = P.Kpad / TC_BK;
     const int kb0 = (int)((int64_t)rank * nkb_all / ks), kb1 = (int)((int64_t)(rank + 1) * nkb_all / ks);
@@ -731,25 +743,39 @@ cudaError_t set_smem_attr() {
 
 template <int S, int BN>
 cudaError_t launch_tc(TcLaunch& L, int total_tiles, cudaStream_t s) {
-    if (L.ks <= 1) {
-        k_gemm_tc<S, BN><<<total_tiles, TC_THREADS2, TcSmem<S, BN>::kBytes, s>>>(L);
-        return cudaGetLastError();
-    }
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
-    cfg.gridDim = dim3((unsigned)(total_tiles * L.ks));
+    cfg.gridDim = dim3((unsigned)(total_tiles * (L.ks > 1 ? L.ks : 1)));
     cfg.blockDim = dim3(TC_THREADS2);
     cfg.dynamicSmemBytes = TcSmem<S, BN>::kBytes;
     cfg.stream = s;
+    cudaLaunchAttribute at[2];
+    memset(at, 0, sizeof(at));
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    at[1].id = cudaLaunchAttributeClusterDimension;
+    at[1].val.clusterDim.x = (unsigned)L.ks;
+    at[1].val.clusterDim.y = 1;
+    at[1].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = L.ks > 1 ? 2 : 1;
+    return cudaLaunchKernelEx(&cfg, k_gemm_tc<S, BN>, L);
+}
+
+template <int S>
+cudaError_t launch_split(const SplitLaunch& SL, int ctas, cudaStream_t s) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3((unsigned)ctas);
+    cfg.blockDim = dim3(kSplitThreads);
+    cfg.stream = s;
     cudaLaunchAttribute at[1];
     memset(at, 0, sizeof(at));
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = (unsigned)L.ks;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_gemm_tc<S, BN>, L);
+    return cudaLaunchKernelEx(&cfg, k_split<S>, SL);
 }
 
 std::mutex g_attr_mu;
@@ -925,23 +951,23 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
     }
     if (TL.np == 0) return cudaSuccess;
     if (split_ctas > 0) {
-        prof_before(s);
+        prof_before(s, SGB_KCLASS_SPLIT);
+        cudaError_t e;
         switch (S) {
-            case 3: k_split<3><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
-            case 4: k_split<4><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
-            case 5: k_split<5><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
-            case 6: k_split<6><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
-            default: k_split<7><<<(unsigned)split_ctas, kSplitThreads, 0, s>>>(SL); break;
+            case 3: e = launch_split<3>(SL, (int)split_ctas, s); break;
+            case 4: e = launch_split<4>(SL, (int)split_ctas, s); break;
+            case 5: e = launch_split<5>(SL, (int)split_ctas, s); break;
+            case 6: e = launch_split<6>(SL, (int)split_ctas, s); break;
+            default: e = launch_split<7>(SL, (int)split_ctas, s); break;
         }
         prof_after(SGB_KCLASS_SPLIT, s, 0.0);
-        cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     double fl = 0.0;
     for (int i = 0; i < np; ++i) fl += useful_flops<double>(probs[i]);
     cudaError_t e = tc_prepare();
     if (e != cudaSuccess) return e;
-    prof_before(s);
+    prof_before(s, SGB_KCLASS_GEMM_TC);
     if (bn == 64) {
         switch (S) {
             case 3: e = launch_tc<3, 64>(TL, (int)gemm_tiles, s); break;

@@ -143,7 +143,7 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
 
 // Launch accounting (sgb_prof.cu): call prof_before just before and
 // prof_after just after every kernel launch.
-void prof_before(cudaStream_t s);
+void prof_before(cudaStream_t s, int kclass = -1);
 void prof_after(int kclass, cudaStream_t s, double flops);
 
 }  // namespace sgb

@@ -601,7 +601,7 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
     e = cudaMemsetAsync(bar, 0, 16 * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     void* args[] = {(void*)&a};
-    prof_before(s);
+    prof_before(s, SGB_KCLASS_PANEL);
     e = cudaLaunchCooperativeKernel((const void*)k_factor_panel<T>, dim3(G), dim3(NT), args, 0, s);
     // useful flops: Cholesky of the m x m block + TRSM of the rows below it
     // (+ the triangular inverse)

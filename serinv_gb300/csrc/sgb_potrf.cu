@@ -71,7 +71,7 @@ GemmProb<T> blank_prob() {
 template <typename T>
 cudaError_t potrf_tile(T* tile, int64_t ld, int nb, int zero_cols_right, T* tinv, int32_t* info,
                        int64_t info_row0, cudaStream_t s) {
-    prof_before(s);
+    prof_before(s, SGB_KCLASS_POTRF_TILE);
     k_potrf_tile<T><<<1, NT, 0, s>>>(tile, ld, nb, zero_cols_right, tinv, info, info_row0);
     prof_after(SGB_KCLASS_POTRF_TILE, s, 2.0 * nb * nb * nb / 3.0);
     return cudaGetLastError();
@@ -82,7 +82,7 @@ cudaError_t trtri_tiles_batched(const T* L, int64_t ldl, int64_t strideL, int m,
                                 int64_t ldx, int64_t strideX, cudaStream_t s) {
     if (m <= 0 || batch <= 0) return cudaSuccess;
     dim3 grid((unsigned)ceil_div(m, kTile), (unsigned)batch);
-    prof_before(s);
+    prof_before(s, SGB_KCLASS_TRTRI_TILE);
     k_trtri_tiles<T><<<grid, NT, 0, s>>>(L, ldl, strideL, m, Linv, ldx, strideX);
     prof_after(SGB_KCLASS_TRTRI_TILE, s, (double)batch * m * (double)kTile * kTile / 3.0);
     return cudaGetLastError();

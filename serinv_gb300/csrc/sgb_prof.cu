@@ -23,7 +23,8 @@ struct Rec {
 };
 
 std::atomic<long long> g_launches{0};
-std::atomic<int> g_enabled{0};
+constexpr unsigned kAllClasses = (1u << SGB_KCLASS_COUNT) - 1u;
+std::atomic<unsigned> g_mask{0};  // kernel classes timed
 std::mutex g_mu;
 std::vector<Rec> g_recs;
 std::vector<cudaEvent_t> g_pool;
@@ -55,8 +56,12 @@ bool capturing(cudaStream_t s) {
     return cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
 }
 
-void prof_before(cudaStream_t s) {
-    if (!g_enabled.load(std::memory_order_relaxed) || capturing(s)) return;
+void prof_before(cudaStream_t s, int kclass) {
+    const unsigned mask = g_mask.load(std::memory_order_relaxed);
+    if (mask == 0) return;
+    // launches that do not name their class are timed only when all are
+    if (kclass >= 0 ? !(mask & (1u << kclass)) : mask != kAllClasses) return;
+    if (capturing(s)) return;
     std::lock_guard<std::mutex> lk(g_mu);
     t_start = get_event();
     cudaEventRecord(t_start, s);
@@ -64,7 +69,7 @@ void prof_before(cudaStream_t s) {
 
 void prof_after(int kclass, cudaStream_t s, double flops) {
     g_launches.fetch_add(1, std::memory_order_relaxed);
-    if (!g_enabled.load(std::memory_order_relaxed) || t_start == nullptr) return;
+    if (t_start == nullptr) return;
     std::lock_guard<std::mutex> lk(g_mu);
     cudaEvent_t e = get_event();
     cudaEventRecord(e, s);
@@ -80,10 +85,12 @@ extern "C" {
 
 long long sgb_launch_count(void) { return g_launches.load(); }
 
-int sgb_profile_enable(int on) {
+int sgb_profile_enable(int on) { return sgb_profile_enable_classes(on ? kAllClasses : 0u); }
+
+int sgb_profile_enable_classes(unsigned mask) {
     std::lock_guard<std::mutex> lk(g_mu);
     recycle_locked();
-    g_enabled.store(on ? 1 : 0);
+    g_mask.store(mask & kAllClasses);
     return SGB_OK;
 }
 
