@@ -433,7 +433,9 @@ def bench_batched(args):
     t0 = time.perf_counter()
     ns = autotune_nstreams(work, rhs, precisions=prec, candidates=(8, 16, 32, 64), reps=1)
     tune_s = time.perf_counter() - t0
+    k0 = _lib.launch_count()
     plan = BatchPlan(work, rhs, precisions=prec, nstreams=ns)
+    kernels_per_graph = _lib.launch_count() - k0  # launches captured into the plan's graph
 
     def restore():
         for d, s_ in zip(work, src):
@@ -463,7 +465,8 @@ def bench_batched(args):
             "dtype": "half f32, half " + ("f64 mixed" if args.batch_precision == "mixed" else "f64"),
             "data": "synthetic (torch generator, seed i for matrix i)",
             "config": {"workload": "batch of 256 uneven BTA matrices", "nstreams": ns,
-                       "autotune_s": tune_s, "not_spd": bad}}
+                       "autotune_s": tune_s, "not_spd": bad},
+            "gpu_launches": kernels_per_graph}
     print(json.dumps(line), flush=True)
 
 

@@ -310,7 +310,9 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
     // one cooperative launch per block, except under stream capture (graph
     // plans) and for small blocks, where the launch-based sweep is used
     const bool persistent = cap == cudaStreamCaptureStatusNone && b > 2 * kTile;
-    bool mixed_inverse = S != 0 && persistent;
+    // 7 slices is the accuracy mode: its TRSMs stay FP64 substitutions (the
+    // product with L_ii^{-T} carries kappa(L_ii) times the slice truncation)
+    bool mixed_inverse = S != 0 && S < 7 && persistent;
     // the launch writes only the upper block triangle of L_ii^{-T}
     if (mixed_inverse) SGB_TRY(cudaMemsetAsync(Xinv, 0, sizeof(T) * bb, s));
     auto factor = [&](int64_t i, RowSet<T> r1, RowSet<T> r2) -> int {
