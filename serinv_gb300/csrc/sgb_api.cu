@@ -307,9 +307,14 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
     unsigned* bar = (unsigned*)((char*)ws + L.bar);
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     SGB_TRY(cudaStreamIsCapturing(s, &cap));
-    // one cooperative launch per block, except under stream capture (graph
-    // plans) and for small blocks, where the launch-based sweep is used
-    const bool persistent = cap == cudaStreamCaptureStatusNone && b > 2 * kTile;
+    // one cooperative launch per block (on part of the GPU when captured
+    // into a graph beside other work, if the capturing thread allows it);
+    // small blocks, and captures that do not, use the launch-based sweep
+    // (FP64 only there: an FP32 column block's FP32 arithmetic is cheap, and
+    // its launch-based sweep holds far fewer SMs than the persistent grid)
+    const bool captured = cap != cudaStreamCaptureStatusNone;
+    const int pgrid = captured && sizeof(T) == 8 ? capture_panel_grid() : 0;
+    const bool persistent = (!captured || pgrid > 0) && b > 2 * kTile;
     // 7 slices is the accuracy mode: its TRSMs stay FP64 substitutions (the
     // product with L_ii^{-T} carries kappa(L_ii) times the slice truncation)
     bool mixed_inverse = S != 0 && S < 7 && persistent;
@@ -319,7 +324,8 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
         T* Di = D + i * bb;
         if (mixed_inverse) {
             RowSet<T> none{nullptr, 0, b};
-            cudaError_t e = factor_panel_persistent<T>(Di, b, b, none, none, tinv, bar, cx.status, info, i * b, s, Xinv);
+            cudaError_t e =
+                factor_panel_persistent<T>(Di, b, b, none, none, tinv, bar, cx.status, info, i * b, s, Xinv, pgrid);
             if (e == cudaSuccess) {
                 GemmProb<T> pr[2];
                 int np = 0;
@@ -339,9 +345,9 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
             if (e != cudaErrorNotSupported) return cuda_fail(e);
             mixed_inverse = false;  // too few SMs for the persistent launch
         }
-        cudaError_t e = persistent
-                            ? factor_panel_persistent<T>(Di, b, b, r1, r2, tinv, bar, cx.status, info, i * b, s)
-                            : cudaErrorNotSupported;
+        cudaError_t e = persistent ? factor_panel_persistent<T>(Di, b, b, r1, r2, tinv, bar, cx.status, info, i * b,
+                                                                s, nullptr, pgrid)
+                                   : cudaErrorNotSupported;
         if (e == cudaErrorNotSupported) e = factor_column_block<T>(Di, b, b, r1, r2, tinv, info, i * b, s);
         return e == cudaSuccess ? SGB_OK : cuda_fail(e);
     };

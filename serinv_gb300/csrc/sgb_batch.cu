@@ -16,6 +16,9 @@
 
 #include "sgb_internal.cuh"
 
+// CTAs of a captured column-block launch.
+constexpr int kPlanPanelGrid = 24;
+
 struct sgb_batch_plan {
     int count = 0;
     int nstreams = 0;
@@ -168,6 +171,10 @@ int sgb_batch_plan_create(const sgb_bta* mats, void* const* rhs, const int64_t* 
         e = cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal);
         capturing = e == cudaSuccess;
     }
+    // pobtaf blocks of b > 64 become one cooperative column-block launch of
+    // kPlanPanelGrid CTAs each (a few run side by side); smaller blocks keep
+    // the launch-based tile sweep
+    sgb::set_capture_panel_grid(kPlanPanelGrid);
     if (e == cudaSuccess) e = cudaEventRecord(events[ns], origin);
     for (int k = 0; k < ns && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(streams[k], events[ns], 0);
     // enqueue every matrix on its stream, biggest first within a stream
@@ -192,6 +199,7 @@ int sgb_batch_plan_create(const sgb_bta* mats, void* const* rhs, const int64_t* 
         e = cudaEventRecord(events[k], streams[k]);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(origin, events[k], 0);
     }
+    sgb::set_capture_panel_grid(0);
     if (capturing) {
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(origin, &g);

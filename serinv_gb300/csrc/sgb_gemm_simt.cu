@@ -130,6 +130,159 @@ __global__ void __launch_bounds__(NT) k_gemm_simt(const __grid_constant__ GemmLa
     }
 }
 
+// Skinny products (N <= 8: the solves' right-hand sides).  A 32 x 32 tile
+// would run a K-long dependent FMA chain per output; here each CTA owns 8
+// output rows and all N columns (so even a 256-row product spreads over 32
+// SMs), and the K dimension is spread over the threads: for a row-major
+// op(A) warp w takes row w and its lanes walk k (coalesced, warp-shuffle
+// reduction); for a transposed op(A) a lane takes row lane % 8 and one of
+// 32 interleaved k streams (8 consecutive rows are one 64-byte segment),
+// reduced by shuffles within the warp and through shared memory across the
+// eight warps.  B is staged 256 rows of k at a time.  Reduction orders are
+// fixed, so results are reproducible.
+constexpr int SK_ROWS = 8, SK_NMAX = 8, SK_KC = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_gemm_skinny(const __grid_constant__ GemmLaunch<T> L) {
+    __shared__ T Bs[SK_KC][SK_NMAX];
+    __shared__ T red[NT / 32][SK_ROWS][SK_NMAX];
+    __shared__ T Cs[SK_ROWS][SK_NMAX + 1];
+
+    const int tile = blockIdx.x;
+    int pi = 0;
+#pragma unroll 1
+    for (int q = 1; q < L.np; ++q)
+        if (tile >= L.p[q].tile_begin) pi = q;
+    const GemmProb<T>& P = L.p[pi];
+    const int local = tile - P.tile_begin;
+    const int inst = local / P.tiles_m;
+    const int m0 = (local - inst * P.tiles_m) * SK_ROWS;
+    const int N = P.N;
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    for (int e = tid; e < SK_ROWS * (SK_NMAX + 1); e += NT) Cs[e / (SK_NMAX + 1)][e % (SK_NMAX + 1)] = T(0);
+
+#pragma unroll 1
+    for (int ti = 0; ti < P.nterms; ++ti) {
+        const GemmTerm<T>& t = P.term[ti];
+        const T* A = t.A + (int64_t)inst * t.strideA;
+        const T* B = t.B + (int64_t)inst * t.strideB;
+        int klo = 0, khi = t.K;
+        switch (t.kmode) {
+            case KM_GE_N0: break;
+            case KM_LT_N1: khi = min(t.K, N); break;
+            case KM_GE_M0: klo = m0; break;
+            case KM_LT_M1: khi = min(t.K, m0 + SK_ROWS); break;
+            default: break;
+        }
+#pragma unroll 1
+        for (int kc0 = klo; kc0 < khi; kc0 += SK_KC) {
+            const int kc1 = min(khi, kc0 + SK_KC);
+            __syncthreads();
+            for (int e = tid; e < (kc1 - kc0) * N; e += NT) {
+                const int k = e / N, j = e - k * N;
+                Bs[k][j] = B[(int64_t)(kc0 + k) * t.ldb + j];
+            }
+            __syncthreads();
+            T acc[SK_NMAX];
+#pragma unroll
+            for (int j = 0; j < SK_NMAX; ++j) acc[j] = T(0);
+            if (!t.transA) {
+                const int gm = m0 + w;
+                if (gm < P.M) {
+                    const T* Ar = A + (int64_t)gm * t.lda;
+                    for (int k = kc0 + lane; k < kc1; k += 32) {
+                        const T a = Ar[k];
+#pragma unroll
+                        for (int j = 0; j < SK_NMAX; ++j)
+                            if (j < N) acc[j] = fma(a, Bs[k - kc0][j], acc[j]);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < SK_NMAX; ++j) {
+                    if (j >= N) continue;
+                    T v = acc[j];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0) Cs[w][j] += v;
+                }
+            } else {
+                const int r = lane & 7, gm = m0 + r;
+                if (gm < P.M)
+                    for (int k = kc0 + w * 4 + (lane >> 3); k < kc1; k += 32) {
+                        const T a = A[(int64_t)k * t.lda + gm];
+#pragma unroll
+                        for (int j = 0; j < SK_NMAX; ++j)
+                            if (j < N) acc[j] = fma(a, Bs[k - kc0][j], acc[j]);
+                    }
+#pragma unroll
+                for (int j = 0; j < SK_NMAX; ++j) {
+                    T v = acc[j];
+                    v += __shfl_xor_sync(0xffffffffu, v, 8);
+                    v += __shfl_xor_sync(0xffffffffu, v, 16);
+                    if (lane < 8) red[w][lane][j] = v;
+                }
+                __syncthreads();
+                for (int e = tid; e < SK_ROWS * N; e += NT) {
+                    const int rr = e / N, j = e - rr * N;
+                    T v = T(0);
+#pragma unroll
+                    for (int q = 0; q < NT / 32; ++q) v += red[q][rr][j];
+                    Cs[rr][j] += v;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    T* C = P.Cout + (int64_t)inst * P.strideC;
+    const T* Ci = P.Cin ? P.Cin + (int64_t)inst * P.strideCin : nullptr;
+    for (int e = tid; e < SK_ROWS * N; e += NT) {
+        const int r = e / N, j = e - r * N, gm = m0 + r;
+        if (gm >= P.M) continue;
+        T v = P.alpha * Cs[r][j];
+        if (Ci != nullptr && P.beta != T(0)) {
+            const T c = P.transCin ? Ci[(int64_t)j * P.ldcin + gm] : Ci[(int64_t)gm * P.ldcin + j];
+            v = fma(P.beta, c, v);
+        }
+        C[(int64_t)gm * P.ldc + j] = v;
+    }
+}
+
+// Bytes an operand of `rows` x `cols` (leading dimension ld) spans over the
+// batch, as [lo, hi).
+template <typename T>
+void span(const T* p, int64_t rows, int64_t cols, int64_t ld, int64_t stride, int32_t batch, uintptr_t& lo,
+          uintptr_t& hi) {
+    lo = (uintptr_t)p;
+    hi = lo + (uintptr_t)(((rows - 1) * ld + cols + (int64_t)(batch - 1) * stride) * (int64_t)sizeof(T));
+}
+
+// The skinny kernel serves a launch when every problem has N <= 8, no
+// transposed B, no lower-only restriction, and no operand overlapping its
+// output (each CTA reads all of B while others write their rows of C).
+template <typename T>
+bool skinny_ok(const GemmProb<T>* probs, int np) {
+    bool any = false;
+    for (int i = 0; i < np; ++i) {
+        const GemmProb<T>& p = probs[i];
+        if (p.M <= 0 || p.N <= 0 || p.batch <= 0) continue;
+        if (p.N > SK_NMAX || p.lower_only) return false;
+        any = true;
+        uintptr_t clo, chi;
+        span(p.Cout, p.M, p.N, p.ldc, p.strideC, p.batch, clo, chi);
+        for (int t = 0; t < p.nterms; ++t) {
+            const GemmTerm<T>& g = p.term[t];
+            if (g.transB) return false;
+            uintptr_t lo, hi;
+            span(g.B, g.K, p.N, g.ldb, g.strideB, p.batch, lo, hi);
+            if (lo < chi && clo < hi) return false;
+            if (g.transA) span(g.A, g.K, p.M, g.lda, g.strideA, p.batch, lo, hi);
+            else span(g.A, p.M, g.K, g.lda, g.strideA, p.batch, lo, hi);
+            if (lo < chi && clo < hi) return false;
+        }
+    }
+    return any;
+}
+
 }  // namespace
 
 template <typename T>
@@ -168,11 +321,12 @@ cudaError_t gemm_simt(GemmProb<T>* probs, int np, cudaStream_t s) {
     GemmLaunch<T> L;
     L.np = 0;
     int64_t total = 0;
+    const bool skinny = skinny_ok<T>(probs, np);
     for (int i = 0; i < np; ++i) {
         GemmProb<T> p = probs[i];
         if (p.M <= 0 || p.N <= 0 || p.batch <= 0) continue;
-        p.tiles_m = (int32_t)ceil_div(p.M, BM);
-        p.tiles_n = (int32_t)ceil_div(p.N, BN);
+        p.tiles_m = (int32_t)ceil_div(p.M, skinny ? SK_ROWS : BM);
+        p.tiles_n = skinny ? 1 : (int32_t)ceil_div(p.N, BN);
         p.tile_begin = (int32_t)total;
         total += (int64_t)p.tiles_m * p.tiles_n * p.batch;
         L.p[L.np++] = p;
@@ -184,7 +338,8 @@ cudaError_t gemm_simt(GemmProb<T>* probs, int np, cudaStream_t s) {
     double fl = 0.0;
     for (int i = 0; i < L.np; ++i) fl += useful_flops<T>(L.p[i]);
     prof_before(s, SGB_KCLASS_GEMM);
-    k_gemm_simt<T><<<(unsigned)total, NT, 0, s>>>(L);
+    if (skinny) k_gemm_skinny<T><<<(unsigned)total, NT, 0, s>>>(L);
+    else k_gemm_simt<T><<<(unsigned)total, NT, 0, s>>>(L);
     prof_after(SGB_KCLASS_GEMM, s, fl);
     return cudaGetLastError();
 }

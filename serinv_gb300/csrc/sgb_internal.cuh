@@ -111,10 +111,20 @@ using GemmFn = cudaError_t (*)(void* ctx, GemmProb<T>* probs, int np, cudaStream
 // them); the tiles strictly below the diagonal tiles are not written, so
 // the caller zeroes them once.  Not for use under stream capture
 // (cooperative launch).
+// `grid_cap` > 0 limits the grid (a launch captured beside others in a
+// graph takes only part of the GPU).
 template <typename T>
 cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, RowSet<T> r2, T* tinv,
                                     unsigned* bar, int32_t* status, int32_t* info, int64_t info_row0,
-                                    cudaStream_t s, T* xinv = nullptr);
+                                    cudaStream_t s, T* xinv = nullptr, int grid_cap = 0);
+
+// Grid of the column-block kernel in sweeps captured by this host thread
+// (0: captured sweeps use the launch-based tile sweep).  Batch plans set it
+// for the duration of their capture; a non-zero value also tells the
+// tensor-core products that the captured launches share the GPU with other
+// streams (no K split across clusters).
+void set_capture_panel_grid(int ctas);
+int capture_panel_grid();
 
 // Full triangular inverse of `batch` lower-triangular m x m blocks:
 // Linv_j = L_j^{-1} (zeros above the diagonal).  Scratch: batch*m*m T.
@@ -144,6 +154,8 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
 // Launch accounting (sgb_prof.cu): call prof_before just before and
 // prof_after just after every kernel launch.
 void prof_before(cudaStream_t s, int kclass = -1);
+// True while `s` is being captured into a graph.
+bool capturing(cudaStream_t s);
 void prof_after(int kclass, cudaStream_t s, double flops);
 
 }  // namespace sgb

@@ -565,7 +565,7 @@ int g_panel_grid[64] = {};
 template <typename T>
 cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, RowSet<T> r2, T* tinv,
                                     unsigned* bar, int32_t* status, int32_t* info, int64_t info_row0,
-                                    cudaStream_t s, T* xinv) {
+                                    cudaStream_t s, T* xinv, int grid_cap) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -579,8 +579,8 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
         if (per < 1) return cudaErrorLaunchOutOfResources;
         g_panel_grid[dev] = sms * per;
     }
-    const int G = g_panel_grid[dev];
-    if (G < kW0 + 8) return cudaErrorNotSupported;  // too few SMs: callers use the launch-based sweep
+    const int G = (grid_cap > 0 && grid_cap < g_panel_grid[dev]) ? grid_cap : g_panel_grid[dev];
+    if (G < kW0 + 8) return cudaErrorNotSupported;  // too few CTAs: callers use the launch-based sweep
     PanelArgs<T> a;
     a.diag = diag;
     a.m = m;
@@ -613,9 +613,15 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
 
 template cudaError_t factor_panel_persistent<double>(double*, int64_t, int64_t, RowSet<double>, RowSet<double>,
                                                      double*, unsigned*, int32_t*, int32_t*, int64_t, cudaStream_t,
-                                                     double*);
+                                                     double*, int);
 template cudaError_t factor_panel_persistent<float>(float*, int64_t, int64_t, RowSet<float>, RowSet<float>,
                                                     float*, unsigned*, int32_t*, int32_t*, int64_t, cudaStream_t,
-                                                    float*);
+                                                    float*, int);
+
+namespace {
+thread_local int t_capture_panel_grid = 0;
+}
+void set_capture_panel_grid(int ctas) { t_capture_panel_grid = ctas < 0 ? 0 : ctas; }
+int capture_panel_grid() { return t_capture_panel_grid; }
 
 }  // namespace sgb

@@ -100,3 +100,31 @@ def test_autotuner_picks_a_candidate(tmp_path, monkeypatch):
         for x, y in zip(d, b):
             assert torch.equal(x, y)
     assert (tmp_path / "tune.json").exists()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_column_block_kernel_in_graph(precision):
+    """Blocks of b > 64 run the cooperative column-block kernel inside the
+    plan's graph (several side by side on part of the GPU)."""
+    rng = np.random.default_rng(21)
+    mats = []
+    for i in range(8):
+        n = int(rng.integers(2, 6))
+        b = int(rng.choice([96, 128, 160]))
+        a = int(rng.choice([0, 16]))
+        dt = np.float32 if (i % 2 == 0 and precision == "fp64") else np.float64
+        mats.append(generate(n, b, a, 4, seed=100 + i, dtype=dt))
+    dev = [tuple(torch.from_numpy(x).cuda() for x in m.arrays()) for m in mats]
+    rhs = [torch.from_numpy(m.B).cuda() for m in mats]
+    plan = BatchPlan(dev, rhs, precisions=[precision] * len(mats), nstreams=4)
+    plan.run()
+    torch.cuda.synchronize()
+    assert torch.all(plan.info() == 0)
+    for m, d, r in zip(mats, dev, rhs):
+        L, X, x = oracle_run(m)
+        tol = TOL[m.D.dtype] if precision == "fp64" else 1e-9
+        for got, ref in zip(d, X):
+            if ref.size:
+                assert rel_err(got.cpu().numpy(), ref) <= tol
+        assert rel_err(r.cpu().numpy(), x) <= tol
+    plan.close()
