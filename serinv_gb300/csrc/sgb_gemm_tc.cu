@@ -343,7 +343,9 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+// 16 consecutive TMEM columns of this warp's 32 lanes; the caller issues
+// tmem_wait_ld before using the values (several loads share one wait).
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, float (&v)[16]) {
     uint32_t r[16];
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
@@ -352,9 +354,28 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
           "=r"(r[15])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// The NACC level accumulators of 16 columns (one wait for all of them).
+template <int NACC, int BN>
+__device__ __forceinline__ void tmem_levels16(uint32_t ta, float (&v)[NACC][16]) {
+#pragma unroll
+    for (int l = 0; l < NACC; ++l) tmem_ld16_async(ta + l * BN, v[l]);
+    tmem_wait_ld();
+}
+
+// 16 bytes from the shared memory of a CTA of this cluster (raddr 16-byte aligned).
+__device__ __forceinline__ float4 ld_dsmem4(uint32_t raddr) {
+    float4 v;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(raddr)
+                 : "memory");
+    return v;
 }
 
 // FP32 -> FP64 by bit operations (exact; zero and subnormal inputs give 0):
@@ -599,26 +620,37 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         hi = h2;
         return scale_pow2(f32_to_f64(hi) + f32_to_f64(lo), eAm + eBn - 2058);
     };
-    // rows [r_lo, r_hi) of the tile are staged in Ds[row - r_lo][col] and written by this CTA
-    int r_lo = 0, r_hi = TC_BM;
-    double* Ds;
+    const bool neg = P.alpha == -1.0, unit = P.alpha == 1.0 || neg;
+    // alpha, beta and C_in applied to one finished element
+    auto store = [&](int row, int col, double r) {
+        const int m = m0 + row, n = n0 + col;
+        if (m >= P.M || n >= P.N || (P.lower_only && n > m)) return;
+        if (!unit) r *= P.alpha;
+        else if (neg) r = -r;
+        if (Ci != nullptr && P.beta != 0.0) {
+            const double cv = P.transCin ? Ci[(int64_t)n * P.ldcin + m] : Ci[(int64_t)m * P.ldcin + n];
+            r = fma(P.beta, cv, r);
+        }
+        C[(int64_t)m * P.ldc + n] = r;
+    };
     if (ks > 1) {
         // K split over the cluster: each CTA parks its level accumulators in
-        // its (now idle) stage memory as R[l][col][row]; after a cluster
-        // barrier CTA q sums rows [q*128/ks, (q+1)*128/ks) over all CTAs
-        // through distributed shared memory -- exact, the level sums being
-        // integers below 2^24 units over the whole K.
+        // its (now idle) stage memory as R[level][row][col] (16-byte stores,
+        // row stride BN + 4); after a cluster barrier CTA q sums rows
+        // [q*nq, (q+1)*nq) over all CTAs through distributed shared memory,
+        // four columns per 16-byte load, every load of an element group in
+        // flight together -- exact, the level sums being integers below
+        // 2^24 units over the whole K -- and writes them out, consecutive
+        // threads on consecutive column groups.
+        constexpr int LD = BN + 4;
         float* R = (float*)smem;
-        Ds = (double*)(smem + NACC * TC_BM * BN * 4);
         if (all_ok && warp < 4) {
             const int row = warp * 32 + lane;
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 float v[NACC][16];
-                const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + c0;
                 if (nkb > 0) {
-#pragma unroll
-                    for (int l = 0; l < NACC; ++l) tmem_ld16(ta + l * BN, v[l]);
+                    tmem_levels16<NACC, BN>(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
                 } else {
 #pragma unroll
                     for (int l = 0; l < NACC; ++l)
@@ -628,61 +660,62 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
 #pragma unroll
                 for (int l = 0; l < NACC; ++l)
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) R[(l * BN + c0 + i) * TC_BM + row] = v[l][i];
+                    for (int i = 0; i < 16; i += 4)
+                        *reinterpret_cast<float4*>(&R[(l * TC_BM + row) * LD + c0 + i]) =
+                            make_float4(v[l][i], v[l][i + 1], v[l][i + 2], v[l][i + 3]);
             }
         }
         cluster_sync_all();
-        r_lo = (int)(rank * TC_BM / ks);
-        r_hi = (int)((rank + 1) * TC_BM / ks);
-        const int nr = r_hi - r_lo;
+        const int nq = (TC_BM + ks - 1) / ks;
+        const int r_lo = (int)rank * nq;
+        const int nr = (r_lo + nq <= TC_BM ? nq : TC_BM - r_lo);
         uint32_t rb[kTcMaxSplit];
 #pragma unroll
         for (int q = 0; q < kTcMaxSplit; ++q) rb[q] = q < ks ? dsmem_addr(smem_u32(R), (uint32_t)q) : 0u;
-        // two elements per pass, all their remote loads in flight together
+        constexpr int G4 = BN / 4;
+        if (all_ok) {
 #pragma unroll 1
-        for (int e = tid; e < nr * BN; e += 2 * TC_THREADS2) {
-            float acc[2][NACC][kTcMaxSplit];
+            for (int g = tid; g < nr * G4; g += TC_THREADS2) {
+                const int row = r_lo + g / G4, c4 = (g % G4) * 4;
+                float4 part[kTcMaxSplit][NACC];
 #pragma unroll
-            for (int hh = 0; hh < 2; ++hh) {
-                const int eh = e + hh * TC_THREADS2;
-                const int row = r_lo + eh % nr, col = eh / nr;
-                const bool in = eh < nr * BN;
+                for (int q = 0; q < kTcMaxSplit; ++q)
 #pragma unroll
-                for (int l = 0; l < NACC; ++l)
-#pragma unroll
-                    for (int q = 0; q < kTcMaxSplit; ++q)
-                        acc[hh][l][q] = (in && q < ks)
-                                            ? ld_dsmem(rb[q] + (uint32_t)(((l * BN + col) * TC_BM + row) * 4))
-                                            : 0.f;
-            }
-#pragma unroll
-            for (int hh = 0; hh < 2; ++hh) {
-                const int eh = e + hh * TC_THREADS2;
-                if (eh >= nr * BN) break;
-                const int row = r_lo + eh % nr, col = eh / nr;
-                float vv[NACC];
+                    for (int l = 0; l < NACC; ++l)
+                        part[q][l] = q < ks ? ld_dsmem4(rb[q] + (uint32_t)(((l * TC_BM + row) * LD + c4) * 4))
+                                            : make_float4(0.f, 0.f, 0.f, 0.f);
+                float vv[4][NACC];
 #pragma unroll
                 for (int l = 0; l < NACC; ++l) {
-                    float t = 0.f;
+                    float4 t = part[0][l];
 #pragma unroll
-                    for (int q = 0; q < kTcMaxSplit; ++q) t += acc[hh][l][q];
-                    vv[l] = t;
+                    for (int q = 1; q < kTcMaxSplit; ++q) {
+                        t.x += part[q][l].x;
+                        t.y += part[q][l].y;
+                        t.z += part[q][l].z;
+                        t.w += part[q][l].w;
+                    }
+                    vv[0][l] = t.x;
+                    vv[1][l] = t.y;
+                    vv[2][l] = t.z;
+                    vv[3][l] = t.w;
                 }
-                Ds[(row - r_lo) * (BN + 1) + col] = combine(vv, eAs[row], eBs[col]);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) store(row, c4 + j, combine(vv[j], eAs[row], eBs[c4 + j]));
             }
         }
+        cluster_sync_all();  // peers are done reading this CTA's accumulators
     } else {
-        Ds = (double*)smem;
+        // the whole K here: TMEM -> FP64 tile in shared memory -> coalesced writes
+        double* Ds = (double*)smem;
         if (all_ok && warp < 4) {
             const int row = warp * 32 + lane;
             const int eAm = eAs[row];
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 float v[NACC][16];
-                const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + c0;
                 if (nkb > 0) {
-#pragma unroll
-                    for (int l = 0; l < NACC; ++l) tmem_ld16(ta + l * BN, v[l]);
+                    tmem_levels16<NACC, BN>(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
                 } else {
 #pragma unroll
                     for (int l = 0; l < NACC; ++l)
@@ -698,27 +731,15 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
                 }
             }
         }
-    }
-    __syncthreads();
-    if (all_ok) {
-        const int nr = r_hi - r_lo;
-        const bool neg = P.alpha == -1.0, unit = P.alpha == 1.0 || neg;
+        __syncthreads();
+        if (all_ok) {
 #pragma unroll 1
-        for (int e = tid; e < nr * BN; e += TC_THREADS2) {
-            const int row = r_lo + e / BN, col = e % BN;
-            const int m = m0 + row, n = n0 + col;
-            if (m >= P.M || n >= P.N || (P.lower_only && n > m)) continue;
-            double r = Ds[(row - r_lo) * (BN + 1) + col];
-            if (!unit) r *= P.alpha;
-            else if (neg) r = -r;
-            if (Ci != nullptr && P.beta != 0.0) {
-                const double cv = P.transCin ? Ci[(int64_t)n * P.ldcin + m] : Ci[(int64_t)m * P.ldcin + n];
-                r = fma(P.beta, cv, r);
+            for (int e = tid; e < TC_BM * BN; e += TC_THREADS2) {
+                const int row = e / BN, col = e % BN;
+                store(row, col, Ds[row * (BN + 1) + col]);
             }
-            C[(int64_t)m * P.ldc + n] = r;
         }
     }
-    if (ks > 1) cluster_sync_all();  // peers may still read this CTA's accumulators
     if (!all_ok && tid == 0) {
         // drain (bounded): the final commit, then any stage still being filled
         mbar_wait(smem_u32(done), 0);
