@@ -81,7 +81,7 @@ struct SplitJob {
     int32_t strips, strip_begin;  // kSplitRows-row strips per instance; first CTA of the job
 };
 
-constexpr int kSplitRows = 4;
+constexpr int kSplitRows = 8;
 constexpr int kSplitThreads = 512;  // two CTAs per SM, eight warps per scheduler: latency bound
 constexpr int kSplitLd = kTcMaxK + 1;  // odd stride: conflict-free row and column access
 
@@ -137,12 +137,6 @@ __device__ __forceinline__ void digits(double x, int Erow, int (&d)[S]) {
     d[0] = hi;
 }
 
-// One CTA per strip of kSplitRows rows of one operand instance: the whole
-// strip (all terms, K <= kTcMaxK) is staged in shared memory with coalesced
-// loads, each row's largest exponent is found by one warp, and the S slices
-// of every element are written in the chunk layout the MMA descriptors
-// read -- padding rows and the K padding of each term as zeros, so the
-// buffers need no clearing beforehand.
 // Programmatic dependent launch: the kernels of a product are launched
 // with programmatic stream serialization, so a launch may start while its
 // predecessor in the stream drains.  Every kernel waits for the
@@ -153,6 +147,12 @@ __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// One CTA per strip of kSplitRows rows of one operand instance: the whole
+// strip (all terms, K <= kTcMaxK) is staged in shared memory with coalesced
+// loads, each row's largest exponent is found by one warp, and the S slices
+// of every element are written in the chunk layout the MMA descriptors
+// read -- padding rows and the K padding of each term as zeros, so the
+// buffers need no clearing beforehand.
 template <int S>
 __global__ void __launch_bounds__(kSplitThreads) k_split(const __grid_constant__ SplitLaunch L) {
     __shared__ double t[kSplitRows][kSplitLd];
@@ -191,8 +191,8 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(const __grid_constant__
                     if (k < Kp) t[rr][src.koff + k] = v[rr][u];
                 }
         } else {
-            constexpr int KS = kSplitThreads / kSplitRows;  // 128 k per pass
-            constexpr int KU = (kTcMaxK + KS - 1) / KS;     // 5
+            constexpr int KS = kSplitThreads / kSplitRows;  // 64 k per pass
+            constexpr int KU = (kTcMaxK + KS - 1) / KS;     // 9
             const int rr = tid % kSplitRows, r = r0 + rr;
             double v[KU];
 #pragma unroll
