@@ -146,7 +146,7 @@ int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char tran
  * SGB_PREC_NATIVE computes.
  *
  * Its scratch is a static device array of sgb_pobtaf_noalloc_scratch_bytes()
- * bytes (64 KiB) that every GPU loading the library keeps until the process
+ * bytes (128 KiB) that every GPU loading the library keeps until the process
  * exits.  Requests whose workspace (sgb_pobtaf_workspace_size) exceeds it
  * return SGB_ERR_WORKSPACE.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress) with that device current; make that

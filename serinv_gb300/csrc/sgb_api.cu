@@ -161,7 +161,7 @@ struct PobtafWs {
         Carve c;
         status = c.take(256);
         bar = c.take(256);
-        tinv = c.take(sizeof(T) * (7 * kTile * kTile + 6 * kTile));  // column-block kernel scratch
+        tinv = c.take(sizeof(T) * (10 * kTile * kTile + 9 * kTile));  // column-block kernel scratch
         const int64_t mx = m->b > m->a ? m->b : m->a;
         tc_bytes = S ? tc_bound(S, mx, m->b, 3) : 0;
         tc = c.take(tc_bytes);

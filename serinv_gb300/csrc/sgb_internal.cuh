@@ -103,7 +103,7 @@ template <typename T>
 using GemmFn = cudaError_t (*)(void* ctx, GemmProb<T>* probs, int np, cudaStream_t s);
 
 // The same column-block factorization as one cooperative persistent launch
-// (sgb_panel.cu).  `tinv` is 7 * kTile * kTile + 6 * kTile elements of
+// (sgb_panel.cu).  `tinv` is 10 * kTile * kTile + 9 * kTile elements of
 // scratch, `bar` 16 unsigned words; `status` receives
 // SGB_ERR_TIMEOUT if a grid barrier gives up.  With `xinv` (m x m,
 // row-major, ld m) the launch also writes L^{-T} there: its upper block

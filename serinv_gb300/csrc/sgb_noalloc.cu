@@ -21,7 +21,7 @@
 
 namespace {
 
-constexpr size_t kStaticScratchBytes = 64 * 1024;
+constexpr size_t kStaticScratchBytes = 128 * 1024;
 constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_pobtaf_scratch[kStaticScratchBytes];

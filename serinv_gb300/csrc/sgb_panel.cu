@@ -69,7 +69,8 @@ struct PanelArgs {
     T* xinv;  // m x m, row-major (ld xld): L^{-T} out, or null
     int64_t xld;
     T* scratch;  // [3][32][32] M^T by column, [3][32] d, [3][32] d^{-1/2},
-                 // [2][32][32] staged diagonal tiles, [2][32][32] staged tile-rows
+                 // [2][32][32] staged diagonal tiles, [2][32][32] staged tile-rows,
+                 // [3][32 * 32 + 32] staged columns of M and d
     int32_t* info;
     int64_t row0;
     unsigned* bar;    // [0] F, [1] I, [4] barrier B, [6] barrier C, [8] columns of M
@@ -133,7 +134,6 @@ __device__ __forceinline__ bool wait_count(const unsigned* ctr, unsigned target,
                 break;
             }
         }
-        __threadfence();
         *sflag = ok;
     }
     __syncthreads();
@@ -231,6 +231,62 @@ __device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T
     return true;
 }
 
+// The helpers' rows: as trsm_row_pipe, with the columns of M and the pivots
+// taken by value from the factorizer's staging buffer vc ([32][32] M^T by
+// column, then [32] d) as they land -- no counter, no fence in between.
+// Up to eight columns are polled at once; the leading ones every lane holds
+// are applied.  d^{-1/2} is formed here, lane by lane, as the pivots
+// arrive.  The result also goes to the staging row.  Returns false on a
+// timeout or an error raised elsewhere.
+template <typename T>
+__device__ __forceinline__ bool trsm_row_vals(T* rp, int w, const T* vc, int32_t* status, T* stage_row) {
+    const int tx = threadIdx.x & 31;
+    T y = tx < w ? ldcg(rp + tx) : T(0);
+    T r = T(0);
+    int k = 0;
+    long long rounds = 0;
+    while (k < w) {
+        const int nb = (w - k) < 8 ? (w - k) : 8;
+        decltype(Staged<T>::ld(vc)) raw[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) raw[u] = u < nb ? Staged<T>::ld(vc + (k + u) * kTile + tx) : Staged<T>::kSentinel;
+        int navail = 0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (navail == u && u < nb && __all_sync(0xffffffffu, raw[u] != Staged<T>::kSentinel)) navail = u + 1;
+        if (navail == 0) {
+            if (++rounds > kBarrierSpin || ((rounds & 63) == 0 && status_bad(status))) {
+                atomicExch(status, SGB_ERR_TIMEOUT);
+                return false;
+            }
+            continue;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (u < navail) {
+                const T yk = __shfl_sync(0xffffffffu, y, k + u);
+                if (tx > k + u) y = fma(-yk, Staged<T>::val(raw[u]), y);
+            }
+        }
+        if (tx >= k && tx < k + navail) {
+            T d;
+            const T* dp[1] = {vc + kTile * kTile + tx};
+            const bool want[1] = {true};
+            T dv[1];
+            if (!stage_take<T, 1>(dp, want, dv, kBarrierSpin, status)) atomicExch(status, SGB_ERR_TIMEOUT);
+            d = dv[0];
+            r = rsq<T>(d);
+        }
+        k += navail;
+    }
+    if (tx < w) {
+        const T x = y * r;
+        rp[tx] = x;
+        stage_put(stage_row + tx, x);
+    }
+    return true;
+}
+
 // dst[32 x 32] <- rows x cols block of a row-major source (zero padded);
 // each thread issues its four loads before storing any.
 template <typename T>
@@ -283,13 +339,15 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
     T* rg = dg + 3 * kTile;                 // [3][32] d^{-1/2}
     T* stT = rg + 3 * kTile;                // [2][32*32] tile (p, p) after its last update, by value
     T* stL = stT + 2 * kTile * kTile;       // [2][32*32] tile-row p+1 in column block p, by value
+    constexpr int kVc = kTile * kTile + kTile;
+    T* stV = stL + 2 * kTile * kTile;       // [3][32*32 + 32] columns of M and d of tile p, by value
     auto tile_w = [&](int64_t p) -> int { return (int)((m - p * kTile) < kTile ? (m - p * kTile) : kTile); };
 
     if (cta == 0) {
         // ---------------- factorizer
         // staging buffers to the sentinel before the first column is
         // published (every later hand-off is ordered after it)
-        for (int e = tid; e < 4 * kTile * kTile; e += NT) stage_clear(stT + e);
+        for (int e = tid; e < 4 * kTile * kTile + 3 * kVc; e += NT) stage_clear(stT + e);
         __syncthreads();
         for (int64_t p = 0; p < nt; ++p) {
             const int64_t c0 = p * kTile;
@@ -301,7 +359,8 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
             factor_tile_m<T>(S, a.diag + c0 * a.ldd + c0, a.ldd, w, a.info, a.row0 + c0, Mg + buf * kTile * kTile,
                              dg + buf * kTile, rg + buf * kTile, CC, (unsigned)(p * kTile),
                              p >= 1 ? stT + (p & 1) * kTile * kTile : nullptr,
-                             p >= 1 ? stL + ((p - 1) & 1) * kTile * kTile : nullptr, a.status);
+                             p >= 1 ? stL + ((p - 1) & 1) * kTile * kTile : nullptr, a.status, stV + (p % 3) * kVc,
+                             p >= 1 ? stV + ((p - 1) % 3) * kVc : nullptr);
             if (!cta_ok(a.status, &S.flag)) return;
             signal(F);
         }
@@ -349,16 +408,14 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
             // column by column as the factorizer publishes M; a timeout sets
             // the status word, which the wait below sees
             T* sL = stL + (p & 1) * kTile * kTile;
+            // The staging buffers of this step were reset during tiles p-2
+            // (columns) and p-1 (tile-row), each ordered before tile p's
+            // first published columns: acquire those before any poll.
+            if (!wait_count(CC, (unsigned)(p * kTile + 1), a.status, &S.flag)) return;
             if (ty < kHelpRows) {
                 const int r = h * kHelpRows + ty;
-                if (r < w2)
-                    trsm_row_pipe<T>(a.diag + (c1 + r) * a.ldd + c0, w, Mp, rp3, CC, (unsigned)(p * kTile), a.status,
-                                     false, -1, sL + r * kTile);
+                if (r < w2) trsm_row_vals<T>(a.diag + (c1 + r) * a.ldd + c0, w, stV + (p % 3) * kVc, a.status, sL + r * kTile);
             }
-            // The staging row buffer was reset during tile p-1, ordered
-            // before tile p's columns: acquire one of those (done already
-            // where this CTA had rows to solve) before any thread polls it.
-            if (!wait_count(CC, (unsigned)(p * kTile + 1), a.status, &S.flag)) return;
             // this thread's element of tile (p+1, p+1) (last written by this CTA)
             const int rr1 = h * kHelpRows + ty, cc1 = tx;
             const bool own1 = ty < kHelpRows && rr1 < w2 && cc1 <= rr1;
@@ -376,14 +433,17 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                     sp[u] = sL + e;
                     want[u] = e / kTile < w2 && e % kTile < w;
                 }
-                if (!stage_take<T, U>(sp, want, v, kBarrierSpin, a.status)) atomicExch(a.status, SGB_ERR_TIMEOUT);
+                const bool took = stage_take<T, U>(sp, want, v, kBarrierSpin, a.status);
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int e = tid + u * NT;
                     S.tmp[e / kTile][e % kTile] = want[u] ? v[u] : T(0);
                 }
+                if (__syncthreads_or(!took)) {
+                    if (tid == 0) atomicExch(a.status, SGB_ERR_TIMEOUT);
+                    return;
+                }
             }
-            if (!cta_ok(a.status, &S.flag)) return;
             if (own1)
                 stage_put(stT + ((p + 1) & 1) * kTile * kTile + rr1 * kTile + cc1,
                           cold - dot32<T>(&S.tmp[rr1][0], &S.tmp[cc1][0], w));

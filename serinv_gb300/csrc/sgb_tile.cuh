@@ -413,7 +413,10 @@ __device__ void factor_tile(Smem<T>& S, T* tile, int64_t ld, int nb, int zero_ri
 // With `staged` the tile's lower part comes from that 32 x 32 staging
 // buffer (ld 32) instead of `tile`, each element taken as its producer
 // stores it and reset to the sentinel; `clear` (32 x 32) is reset to the
-// sentinel; a poll that gives up sets *status = SGB_ERR_TIMEOUT.
+// sentinel; a poll that gives up sets *status = SGB_ERR_TIMEOUT.  With
+// `vcols` warp 5 also hands the factor on by value, without fences: d_k to
+// vcols[1024 + k] and column k of M to vcols[32 k .. 32 k + 31] as the
+// companion finishes them; `vclear` (32 x 32 + 32) is reset first.
 //
 // Pivot <-> companion hand-offs use named barriers PQ (ids 5, 6) and QP
 // (7, 8), READY/UPD ids 1-4 (companion + workers); every pair alternates
@@ -423,7 +426,7 @@ template <typename T>
 __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int32_t* info, int64_t row0,
                               T* mt = nullptr, T* dv = nullptr, T* rv = nullptr, unsigned* colcount = nullptr,
                               unsigned col_base = 0, T* staged = nullptr, T* clear = nullptr,
-                              int32_t* status = nullptr) {
+                              int32_t* status = nullptr, T* vcols = nullptr, T* vclear = nullptr) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     constexpr int kCons = 32 * 5;  // companion + four workers
     constexpr int kPair = 64;
@@ -544,10 +547,29 @@ __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int
             }
         }
     } else if (warp == 5) {
-        // every consumer of `clear` is done with it (they all produced the
-        // staged values taken above)
+        // every consumer of `clear` and `vclear` is done with them (they all
+        // produced the staged values taken above)
         if (clear != nullptr)
             for (int e = lane; e < kTile * kTile; e += 32) stage_clear(clear + e);
+        if (vclear != nullptr)
+            for (int e = lane; e < kTile * kTile + kTile; e += 32) stage_clear(vclear + e);
+        if (vcols != nullptr) {
+            // the columns by value as the companion finishes them: d_k to
+            // vcols[1024 + k], then column k of M to vcols[k * 32 + 0..31]
+            int done = 0;
+            long long spins = 0;
+            while (done < nb) {
+                int avail = 0;
+                for (;;) {
+                    asm volatile("ld.acquire.cta.shared.u32 %0, [%1];" : "=r"(avail) : "r"(smem_u32(&S.pub)) : "memory");
+                    if (avail > done || ++spins > (1ll << 26)) break;
+                }
+                if (avail <= done) break;
+                if (lane >= done && lane < avail) stage_put(vcols + kTile * kTile + lane, S.yv[lane]);
+                for (int k = done; k < avail; ++k) stage_put(vcols + k * kTile + lane, S.x[lane][k]);
+                done = avail;
+            }
+        }
     } else {
         const int wid = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;  // 0..127
         for (int k = 0; k < nb; ++k) {
