@@ -605,20 +605,29 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         else if (tid - TC_BM < BN) eBs[tid - TC_BM] = (n0 + tid - TC_BM < P.N) ? eB[n0 + tid - TC_BM] : 0;
     }
     __syncthreads();
-    auto combine = [&](const float (&vv)[NACC], int eAm, int eBn) -> double {
-        if (eAm == 0 || eBn == 0) return 0.0;
-        float hi = vv[0], lo = 0.f;
-#pragma unroll
-        for (int l = 1; l < NACC; ++l) {
-            const float s2 = hi + vv[l];
-            const float bb = s2 - hi;
-            lo += (hi - (s2 - bb)) + (vv[l] - bb);
-            hi = s2;
-        }
+    // FP32 pair hi + lo of a sum: exact two-sum of every term into hi,
+    // the rounding errors and small terms collected in lo, then normalised
+    auto add2 = [](float& hi, float& lo, float x) {
+        const float s2 = hi + x;
+        const float bb = s2 - hi;
+        lo += (hi - (s2 - bb)) + (x - bb);
+        hi = s2;
+    };
+    auto norm2 = [](float& hi, float& lo) {
         const float h2 = hi + lo;
         lo = lo - (h2 - hi);
         hi = h2;
+    };
+    auto finish = [&](float hi, float lo, int eAm, int eBn) -> double {
+        if (eAm == 0 || eBn == 0) return 0.0;
         return scale_pow2(f32_to_f64(hi) + f32_to_f64(lo), eAm + eBn - 2058);
+    };
+    auto combine = [&](const float (&vv)[NACC], int eAm, int eBn) -> double {
+        float hi = vv[0], lo = 0.f;
+#pragma unroll
+        for (int l = 1; l < NACC; ++l) add2(hi, lo, vv[l]);
+        norm2(hi, lo);
+        return finish(hi, lo, eAm, eBn);
     };
     const bool neg = P.alpha == -1.0, unit = P.alpha == 1.0 || neg;
     // alpha, beta and C_in applied to one finished element
@@ -634,16 +643,17 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         C[(int64_t)m * P.ldc + n] = r;
     };
     if (ks > 1) {
-        // K split over the cluster: each CTA parks its level accumulators in
-        // its (now idle) stage memory as R[level][row][col] (16-byte stores,
-        // row stride BN + 4); after a cluster barrier CTA q sums rows
-        // [q*nq, (q+1)*nq) over all CTAs through distributed shared memory,
-        // four columns per 16-byte load, every load of an element group in
-        // flight together -- exact, the level sums being integers below
-        // 2^24 units over the whole K -- and writes them out, consecutive
-        // threads on consecutive column groups.
-        constexpr int LD = BN + 4;
-        float* R = (float*)smem;
+        // K split over the cluster: each CTA folds its level accumulators of
+        // every element into an FP32 pair hi + lo (exact level sums, the
+        // pair good to ~2^-48 of the partial -- far below the 2^-(7S+1)
+        // slice truncation) and parks the pairs in its (now idle) stage
+        // memory as R2[row][col] (row stride BN + 2 pairs, 16-byte stores);
+        // after a cluster barrier CTA q sums rows [q*nq, (q+1)*nq) over all
+        // CTAs through distributed shared memory, two elements per 16-byte
+        // load, every load of a group in flight together, and writes them
+        // out, consecutive threads on consecutive column pairs.
+        constexpr int LD2 = BN + 2;
+        float2* R2 = (float2*)smem;
         if (all_ok && warp < 4) {
             const int row = warp * 32 + lane;
 #pragma unroll 1
@@ -658,11 +668,17 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
                         for (int i = 0; i < 16; ++i) v[l][i] = 0.f;
                 }
 #pragma unroll
-                for (int l = 0; l < NACC; ++l)
+                for (int i = 0; i < 16; i += 2) {
+                    float h0 = v[0][i], l0 = 0.f, h1 = v[0][i + 1], l1 = 0.f;
 #pragma unroll
-                    for (int i = 0; i < 16; i += 4)
-                        *reinterpret_cast<float4*>(&R[(l * TC_BM + row) * LD + c0 + i]) =
-                            make_float4(v[l][i], v[l][i + 1], v[l][i + 2], v[l][i + 3]);
+                    for (int l = 1; l < NACC; ++l) {
+                        add2(h0, l0, v[l][i]);
+                        add2(h1, l1, v[l][i + 1]);
+                    }
+                    norm2(h0, l0);
+                    norm2(h1, l1);
+                    *reinterpret_cast<float4*>(&R2[row * LD2 + c0 + i]) = make_float4(h0, l0, h1, l1);
+                }
             }
         }
         cluster_sync_all();
@@ -671,37 +687,29 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         const int nr = (r_lo + nq <= TC_BM ? nq : TC_BM - r_lo);
         uint32_t rb[kTcMaxSplit];
 #pragma unroll
-        for (int q = 0; q < kTcMaxSplit; ++q) rb[q] = q < ks ? dsmem_addr(smem_u32(R), (uint32_t)q) : 0u;
-        constexpr int G4 = BN / 4;
+        for (int q = 0; q < kTcMaxSplit; ++q) rb[q] = q < ks ? dsmem_addr(smem_u32(R2), (uint32_t)q) : 0u;
+        constexpr int G2 = BN / 2;
         if (all_ok) {
 #pragma unroll 1
-            for (int g = tid; g < nr * G4; g += TC_THREADS2) {
-                const int row = r_lo + g / G4, c4 = (g % G4) * 4;
-                float4 part[kTcMaxSplit][NACC];
+            for (int g = tid; g < nr * G2; g += TC_THREADS2) {
+                const int row = r_lo + g / G2, c2 = (g % G2) * 2;
+                float4 part[kTcMaxSplit];
 #pragma unroll
                 for (int q = 0; q < kTcMaxSplit; ++q)
+                    part[q] = q < ks ? ld_dsmem4(rb[q] + (uint32_t)((row * LD2 + c2) * 8))
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+                float h0 = part[0].x, l0 = part[0].y, h1 = part[0].z, l1 = part[0].w;
 #pragma unroll
-                    for (int l = 0; l < NACC; ++l)
-                        part[q][l] = q < ks ? ld_dsmem4(rb[q] + (uint32_t)(((l * TC_BM + row) * LD + c4) * 4))
-                                            : make_float4(0.f, 0.f, 0.f, 0.f);
-                float vv[4][NACC];
-#pragma unroll
-                for (int l = 0; l < NACC; ++l) {
-                    float4 t = part[0][l];
-#pragma unroll
-                    for (int q = 1; q < kTcMaxSplit; ++q) {
-                        t.x += part[q][l].x;
-                        t.y += part[q][l].y;
-                        t.z += part[q][l].z;
-                        t.w += part[q][l].w;
-                    }
-                    vv[0][l] = t.x;
-                    vv[1][l] = t.y;
-                    vv[2][l] = t.z;
-                    vv[3][l] = t.w;
+                for (int q = 1; q < kTcMaxSplit; ++q) {
+                    add2(h0, l0, part[q].x);
+                    l0 += part[q].y;
+                    add2(h1, l1, part[q].z);
+                    l1 += part[q].w;
                 }
-#pragma unroll
-                for (int j = 0; j < 4; ++j) store(row, c4 + j, combine(vv[j], eAs[row], eBs[c4 + j]));
+                norm2(h0, l0);
+                norm2(h1, l1);
+                store(row, c2, finish(h0, l0, eAs[row], eBs[c2]));
+                store(row, c2 + 1, finish(h1, l1, eAs[row], eBs[c2 + 1]));
             }
         }
         cluster_sync_all();  // peers are done reading this CTA's accumulators
