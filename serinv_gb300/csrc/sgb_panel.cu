@@ -329,6 +329,10 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
     const int64_t m = a.m;
     const int64_t nt = (m + kTile - 1) / kTile;
     const int tx = tid & 31, ty = tid >> 5;
+    // the next kernel in the stream (a programmatic dependent launch) may
+    // start launching now; it waits for this grid's completion before it
+    // touches memory
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     unsigned* F = a.bar + 0;
     unsigned* I = a.bar + 1;
     unsigned* barB = a.bar + 4;
