@@ -8,7 +8,7 @@ layout, computed by hand-written sm_103a CUDA kernels behind the C ABI in
 
 __version__ = "0.1.0"
 
-from .algs import pobtaf, pobtasi, pobtas  # noqa: E402,F401
+from .algs import pobtaf, pobtasi, pobtas, pobtf, pobtsi, pobts  # noqa: E402,F401
 from .dense import dgemm  # noqa: E402,F401
 
-__all__ = ["pobtaf", "pobtasi", "pobtas", "dgemm", "__version__"]
+__all__ = ["pobtaf", "pobtasi", "pobtas", "pobtf", "pobtsi", "pobts", "dgemm", "__version__"]

@@ -298,3 +298,56 @@ def pobtas(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_a
                             precision, ws.data_ptr(), nbytes.value, _stream(device))
         _lib.raise_for(rc, "pobtas")
         _finish(w)
+
+
+# --------------------------------------------------------------------------
+# block tridiagonal (no arrowhead) family: the same kernels with a = 0
+
+
+def _empty_arrow(D):
+    """Arrow stack (n, 0, b) and tip (0, 0) of D's kind, dtype and device."""
+    if isinstance(D, np.ndarray):
+        return (np.empty((D.shape[0], 0, D.shape[2]), dtype=D.dtype), np.empty((0, 0), dtype=D.dtype))
+    t = D if isinstance(D, torch.Tensor) else torch.from_dlpack(D)
+    return (torch.empty((t.shape[0], 0, t.shape[2]), dtype=t.dtype, device=t.device),
+            torch.empty((0, 0), dtype=t.dtype, device=t.device))
+
+
+def pobtf(A_diagonal_blocks, A_lower_diagonal_blocks, **kwargs):
+    """Cholesky factorization of a block tridiagonal SPD matrix, in place.
+
+    Mirrors src/serinv/algs/pobtf.py:11-80 (kwargs ``device_streaming``,
+    ``buffer`` -- not supported yet, NotImplementedError --,
+    ``factorize_last_block``; unknown keywords raise TypeError, pobtf.py:
+    44-47).  Computes what pobtaf computes with an empty arrowhead.
+    """
+    unexpected = set(kwargs) - _POBTAF_KW - _EXTENSION_KW
+    if unexpected:
+        raise TypeError(f"Unexpected keyword arguments: {unexpected}")
+    Ar, T = _empty_arrow(A_diagonal_blocks)
+    pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, Ar, T, **kwargs)
+
+
+def pobtsi(L_diagonal_blocks, L_lower_diagonal_blocks, **kwargs):
+    """Selected inversion of a block tridiagonal matrix from its Cholesky factor, in place.
+
+    Mirrors src/serinv/algs/pobtsi.py:10-75 (kwargs ``device_streaming``,
+    ``buffer`` -- not supported yet --, ``invert_last_block``; unknown
+    keywords raise TypeError, pobtsi.py:39-42).
+    """
+    unexpected = set(kwargs) - _POBTASI_KW - _EXTENSION_KW
+    if unexpected:
+        raise TypeError(f"Unexpected keyword arguments: {unexpected}")
+    Ar, T = _empty_arrow(L_diagonal_blocks)
+    pobtasi(L_diagonal_blocks, L_lower_diagonal_blocks, Ar, T, **kwargs)
+
+
+def pobts(L_diagonal_blocks, L_lower_diagonal_blocks, B, trans="N", **kwargs):
+    """Triangular solve with the Cholesky factor of a block tridiagonal matrix, in place on ``B``.
+
+    Mirrors src/serinv/algs/pobts.py:10-55 (``trans`` "N", "T" or "C";
+    ``partial``; ``device_streaming`` and ``buffer`` raise
+    NotImplementedError; unknown keywords are ignored, as there).
+    """
+    Ar, T = _empty_arrow(L_diagonal_blocks)
+    pobtas(L_diagonal_blocks, L_lower_diagonal_blocks, Ar, T, B, trans=trans, **kwargs)

@@ -209,3 +209,38 @@ def test_bad_shapes_rejected():
         sg.pobtaf(d[0], d[1][:, :4], d[2], d[3])
     with pytest.raises(ValueError):
         sg.pobtas(*d, dev(np.zeros((5, 1))))
+
+
+BT_CASES = [c for c in CASES if c[1]["Ar"].shape[1] == 0]
+
+
+@pytest.mark.parametrize("case", BT_CASES, ids=[c[0] for c in BT_CASES])
+def test_bt_family_golden(case):
+    """pobtf / pobtsi / pobts (the arrow-free family) against the reference's
+    own pobtf / pobtsi / pobts outputs."""
+    key, inp, L, X, x = case
+    tol = TOL[inp["D"].dtype]
+    d = [dev(inp["D"]), dev(inp["Lo"])]
+    sg.pobtf(*d)
+    Lg = [host(t) for t in d]
+    sg.pobtsi(*d)
+    Xg = [host(t) for t in d]
+    dl = [dev(t) for t in Lg]
+    bt = dev(inp["B"])
+    sg.pobts(*dl, bt, trans="N")
+    sg.pobts(*dl, bt, trans="C")
+    for got, ref in zip(Lg, L[:2]):
+        if ref.size:
+            assert rel_err(got, ref) <= tol
+    for got, ref in zip(Xg, X[:2]):
+        if ref.size:
+            assert rel_err(got, ref) <= tol
+    assert rel_err(host(bt), x) <= tol
+
+
+def test_bt_family_rejects_unknown_kwargs():
+    m = generate(3, 8, 0, 1, seed=1)
+    with pytest.raises(TypeError):
+        sg.pobtf(dev(m.D), dev(m.Lo), bogus=1)
+    with pytest.raises(TypeError):
+        sg.pobtsi(dev(m.D), dev(m.Lo), bogus=1)
