@@ -138,6 +138,32 @@ int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char tran
                void* stream);
 
 /*
+ * Permuted (middle-partition) forms: the `buffer=` keyword of the reference
+ * functions.  buffer (n, b, b) carries the fill-in between block 0 and the
+ * eliminated blocks 1..n-2; blocks 0, n-1 and the tip form the reduced
+ * system that the caller factorizes, inverts or solves itself.  SGB_PREC_NATIVE
+ * only (SGB_ERR_UNSUPPORTED otherwise); n >= 2.
+ *
+ * sgb_pobtaf_permuted: pobtaf(..., buffer=) (src/serinv/algs/pobtaf.py:
+ *   58-76, _pobtaf_permuted :186-281).  Workspace: sgb_pobtaf_workspace_size.
+ *   buffer[1] <- lower[0]^T first; buffer[0] is not touched.
+ * sgb_pobtasi_permuted: pobtasi(..., buffer=) (src/serinv/algs/pobtasi.py:
+ *   54-71, _pobtasi_permuted :175-244).  On entry blocks 0 and n-1, arrow[0],
+ *   arrow[n-1], tip and buffer[n-1] hold the reduced system's inverse.
+ *   Workspace: sgb_pobtasi_permuted_workspace_size.
+ * sgb_pobtas_permuted: pobtas(..., buffer=) (src/serinv/algs/pobtas.py:
+ *   31-46, _pobtas_permuted :164-218).  Workspace: sgb_pobtas_workspace_size.
+ */
+int sgb_pobtaf_permuted(const sgb_bta* m, void* buffer, int precision, void* workspace,
+                        size_t workspace_bytes, int32_t* info, void* stream);
+int sgb_pobtasi_permuted_workspace_size(const sgb_bta* m, int precision, size_t* bytes);
+int sgb_pobtasi_permuted(const sgb_bta* m, void* buffer, int precision, void* workspace,
+                         size_t workspace_bytes, void* stream);
+int sgb_pobtas_permuted(const sgb_bta* m, void* buffer, void* rhs, int64_t nrhs, int64_t ldb,
+                        char trans, int precision, void* workspace, size_t workspace_bytes,
+                        void* stream);
+
+/*
  * sgb_pobtaf without a workspace argument, for callers that cannot allocate
  * device memory: code running while a stream is being captured, real-time
  * loops that forbid allocator calls, and foreign-language hosts that hold

@@ -15,3 +15,4 @@ reference implementation itself (``tests/golden/make_golden.py``), and
 """
 
 from .bta import pobtaf, pobtasi, pobtas, bta_to_dense, dense_to_bta  # noqa: F401
+from .bta import pobtaf_permuted, pobtasi_permuted, pobtas_permuted  # noqa: F401

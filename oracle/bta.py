@@ -1,4 +1,5 @@
-"""NumPy/SciPy restatement of the reference's natural-ordering BTA algorithms.
+"""NumPy/SciPy restatement of the reference's BTA algorithms (natural ordering
+and the permuted middle-partition variants).
 
 Test infrastructure only (see the package docstring): the CUDA product path
 never imports this module.
@@ -113,6 +114,76 @@ def pobtas(D, Lo, Ar, T, B, trans: str = "N", partial: bool = False) -> None:
             if a:
                 rhs = rhs - Ar[i].conj().T @ B[tip]
             B[blk(i)] = la.solve_triangular(D[i], rhs, lower=True, trans="C")
+
+
+def pobtaf_permuted(D, Lo, Ar, T, buf) -> None:
+    """Block Cholesky of a middle partition with the two-sided fill-in column
+    ``buf`` (n, b, b), after ``_pobtaf_permuted`` (src/serinv/algs/pobtaf.py:
+    186-281).  Blocks 1..n-2 are eliminated; block 0 (top), block n-1 and the
+    tip receive the Schur updates and form the reduced system."""
+    n = D.shape[0]
+    buf[1] = Lo[0].conj().T  # pobtaf.py:203
+    for i in range(1, n - 1):  # :206
+        D[i] = _chol(D[i])  # :208
+        Lo[i] = la.solve_triangular(D[i], Lo[i].conj().T, lower=True).conj().T  # :212-220
+        buf[i] = la.solve_triangular(D[i], buf[i].conj().T, lower=True).conj().T  # :223-231
+        Ar[i] = la.solve_triangular(D[i], Ar[i].conj().T, lower=True).conj().T  # :234-242
+        D[i + 1] = D[i + 1] - Lo[i] @ Lo[i].conj().T  # :246-250
+        Ar[i + 1] = Ar[i + 1] - Ar[i] @ Lo[i].conj().T  # :253-256
+        T[:, :] = T - Ar[i] @ Ar[i].conj().T  # :260-263
+        D[0] = D[0] - buf[i] @ buf[i].conj().T  # :267-269
+        buf[i + 1] = -buf[i] @ Lo[i].conj().T  # :272-274
+        Ar[0] = Ar[0] - Ar[i] @ buf[i].conj().T  # :278-281
+
+
+def pobtasi_permuted(D, Lo, Ar, T, buf) -> None:
+    """Selected inversion of a middle partition, after ``_pobtasi_permuted``
+    (src/serinv/algs/pobtasi.py:175-244).  On entry blocks 0, n-1, the tip,
+    ``Ar[0]``, ``Ar[-1]`` and ``buf[-1]`` already hold the selected inverse of
+    the reduced system; blocks n-2..1 are filled in."""
+    n, b = D.shape[0], D.shape[1]
+    eye = np.eye(b, dtype=D.dtype)
+    for i in range(n - 2, 0, -1):  # pobtasi.py:199
+        lo_i = Lo[i].copy()  # :200
+        ar_i = Ar[i].copy()  # :201
+        buf_i = buf[i].copy()  # :202
+        Linv = la.solve_triangular(D[i], eye, lower=True)  # :204-208
+        # :211-216  X_{i+1,i}
+        Lo[i] = (-buf[i + 1].conj().T @ buf_i - D[i + 1] @ lo_i - Ar[i + 1].conj().T @ ar_i) @ Linv
+        # :219-223  X_{top,i}
+        buf[i] = (-buf[i + 1] @ lo_i - D[0] @ buf_i - Ar[0].conj().T @ ar_i) @ Linv
+        # :227-231  X_{A,i}
+        Ar[i] = (-Ar[i + 1] @ lo_i - Ar[0] @ buf_i - T @ ar_i) @ Linv
+        # :234-241  X_{i,i}
+        D[i] = (Linv.conj().T - Lo[i].conj().T @ lo_i - buf[i].conj().T @ buf_i
+                - Ar[i].conj().T @ ar_i) @ Linv
+    Lo[0] = buf[1].conj().T  # :244
+
+
+def pobtas_permuted(D, Lo, Ar, T, B, buf, trans: str = "N") -> None:
+    """Block triangular solve of a middle partition, after ``_pobtas_permuted``
+    (src/serinv/algs/pobtas.py:164-218).  Blocks 1..n-2 are solved; block 0
+    and the tip receive the updates (the reduced system's right-hand side)."""
+    n, b = D.shape[0], D.shape[1]
+    a = Ar.shape[1]
+    tip = slice(n * b, n * b + a)
+
+    def blk(i):
+        return slice(i * b, (i + 1) * b)
+
+    if trans == "N":  # pobtas.py:179
+        for i in range(1, n - 1):
+            B[blk(i)] = la.solve_triangular(D[i], B[blk(i)], lower=True)  # :182-186
+            B[blk(i + 1)] -= Lo[i] @ B[blk(i)]  # :189-192
+            B[blk(0)] -= buf[i] @ B[blk(i)]  # :195-197
+            B[tip] -= Ar[i] @ B[blk(i)]  # :200-203
+    elif trans in ("T", "C"):  # :204-216
+        for i in range(n - 2, 0, -1):
+            rhs = (B[blk(i)] - Lo[i].conj().T @ B[blk(i + 1)] - Ar[i].conj().T @ B[tip]
+                   - buf[i].conj().T @ B[blk(0)])  # :208-212
+            B[blk(i)] = la.solve_triangular(D[i], rhs, lower=True, trans="C")  # :207-216
+    else:
+        raise ValueError(f"Invalid transpose argument: {trans}.")  # :217-218
 
 
 def bta_to_dense(D, Lo, Ar, T, symmetric: bool = True) -> np.ndarray:

@@ -184,15 +184,17 @@ def pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_a
 
     Mirrors src/serinv/algs/pobtaf.py:11-94.  Keyword arguments:
     ``device_streaming`` (accepted; the matrix is processed in HBM),
-    ``buffer`` (permuted middle-partition variant, pobtaf.py:186-281: not
-    supported yet, raises NotImplementedError), ``factorize_last_block``
-    (default True).  Unknown keywords raise TypeError (pobtaf.py:50-53).
+    ``buffer`` (an (n, b, b) array: the permuted middle-partition
+    elimination of pobtaf.py:186-281, storage precision only),
+    ``factorize_last_block`` (default True).  Unknown keywords raise
+    TypeError (pobtaf.py:50-53).
     """
     unexpected = set(kwargs) - _POBTAF_KW - _EXTENSION_KW
     if unexpected:
         raise TypeError(f"Unexpected keyword arguments: {unexpected}")
     if kwargs.get("buffer", None) is not None:
-        raise NotImplementedError("the permuted (buffer=) factorization is not supported yet")
+        return _pobtaf_permuted(A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks,
+                                A_arrow_tip_block, kwargs["buffer"], kwargs)
     factorize_last_block = bool(kwargs.get("factorize_last_block", True))
     precision = _precision(kwargs)
     check = bool(kwargs.get("check_spd", True))
@@ -223,15 +225,16 @@ def pobtasi(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_
     """Selected inversion of a block tridiagonal with arrowhead matrix from its Cholesky factor, in place.
 
     Mirrors src/serinv/algs/pobtasi.py:10-89.  Keyword arguments:
-    ``device_streaming`` (accepted), ``buffer`` (permuted variant: not
-    supported yet), ``invert_last_block`` (default True).  Unknown keywords
-    raise TypeError (pobtasi.py:45-48).
+    ``device_streaming`` (accepted), ``buffer`` (the permuted variant of
+    pobtasi.py:175-244, storage precision only), ``invert_last_block``
+    (default True).  Unknown keywords raise TypeError (pobtasi.py:45-48).
     """
     unexpected = set(kwargs) - _POBTASI_KW - _EXTENSION_KW
     if unexpected:
         raise TypeError(f"Unexpected keyword arguments: {unexpected}")
     if kwargs.get("buffer", None) is not None:
-        raise NotImplementedError("the permuted (buffer=) selected inversion is not supported yet")
+        return _pobtasi_permuted(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks,
+                                 L_arrow_tip_block, kwargs["buffer"], kwargs)
     invert_last_block = bool(kwargs.get("invert_last_block", True))
     precision = _precision(kwargs)
 
@@ -259,18 +262,22 @@ def pobtas(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_a
     Mirrors src/serinv/algs/pobtas.py:10-62: ``trans="N"`` computes
     ``B <- L^{-1} B``, ``"T"``/``"C"`` computes ``B <- L^{-T} B``, anything
     else raises ValueError (pobtas.py:160-161).  ``partial=True`` skips the
-    last diagonal block and the tip.  ``device_streaming`` and ``buffer``
-    raise NotImplementedError (pobtas.py:33-36,49-52; the permuted solve is
-    not supported yet).  Like the reference, unknown keywords are ignored.
-    For arrow width 0 the call is the arrow-free solve of
-    src/serinv/algs/pobts.py:57-118 (the reference's pobtas fails there).
+    last diagonal block and the tip.  ``buffer`` selects the permuted solve
+    of pobtas.py:164-218 (storage precision only).  ``device_streaming``
+    raises NotImplementedError (pobtas.py:33-36,49-52).  Like the reference,
+    unknown keywords are ignored.  For arrow width 0 the call is the
+    arrow-free solve of src/serinv/algs/pobts.py:57-118 (the reference's
+    pobtas fails there).
     """
+    buffer = kwargs.get("buffer", None)
     if kwargs.get("device_streaming", False):
-        raise NotImplementedError("Streaming is not implemented for the natural arrowhead.")
-    if kwargs.get("buffer", None) is not None:
-        raise NotImplementedError("the permuted (buffer=) solve is not supported yet")
+        what = "natural" if buffer is None else "permuted"
+        raise NotImplementedError(f"Streaming is not implemented for the {what} arrowhead.")
     if trans not in ("N", "T", "C"):
         raise ValueError(f"Invalid transpose argument: {trans}.")
+    if buffer is not None:
+        return _pobtas_permuted(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks,
+                                L_arrow_tip_block, B, buffer, trans, kwargs)
     partial = bool(kwargs.get("partial", False))
     precision = _precision(kwargs)
 
@@ -301,6 +308,100 @@ def pobtas(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_a
 
 
 # --------------------------------------------------------------------------
+# permuted (middle-partition) forms: the ``buffer=`` keyword
+
+
+def _native_only(kwargs, what: str) -> int:
+    precision = _precision(kwargs)
+    if precision != _lib.SGB_PREC_NATIVE:
+        raise NotImplementedError(f"{what} with buffer= computes in the storage precision only")
+    return precision
+
+
+def _check_buffer(buf: torch.Tensor, D: torch.Tensor) -> None:
+    n, b = D.shape[0], D.shape[1]
+    if tuple(buf.shape) != (n, b, b):
+        raise ValueError(f"buffer must have shape {(n, b, b)}, got {tuple(buf.shape)}")
+    if buf.dtype != D.dtype:
+        raise TypeError(f"buffer has dtype {buf.dtype}, the blocks have {D.dtype}")
+
+
+def _pobtaf_permuted(D, Lo, Ar, T, buffer, kwargs):
+    """pobtaf(..., buffer=): src/serinv/algs/pobtaf.py:186-281."""
+    precision = _native_only(kwargs, "pobtaf")
+    check = bool(kwargs.get("check_spd", True))
+    lib = _lib.load()
+    device, w = _prepare((D, Lo, Ar, T, buffer),
+                         ("A_diagonal_blocks", "A_lower_diagonal_blocks", "A_lower_arrow_blocks",
+                          "A_arrow_tip_block", "buffer"))
+    _check_buffer(w[4].t, w[0].t)
+    m = _bta_struct(*(x.t for x in w[:4]))
+    with torch.cuda.device(device):
+        nbytes = ctypes.c_size_t(0)
+        _lib.raise_for(lib.sgb_pobtaf_workspace_size(ctypes.byref(m), precision, ctypes.byref(nbytes)),
+                       "pobtaf")
+        ws = _workspace(nbytes.value, device)
+        info = torch.zeros(1, dtype=torch.int32, device=device)
+        rc = lib.sgb_pobtaf_permuted(ctypes.byref(m), _ptr(w[4].t), precision, ws.data_ptr(), nbytes.value,
+                                     info.data_ptr(), _stream(device))
+        _lib.raise_for(rc, "pobtaf")
+        _finish(w)
+        if check:
+            k = int(info.item())
+            if k > 0:
+                raise np.linalg.LinAlgError(f"{k}-th leading minor of the array is not positive definite")
+
+
+def _pobtasi_permuted(D, Lo, Ar, T, buffer, kwargs):
+    """pobtasi(..., buffer=): src/serinv/algs/pobtasi.py:175-244."""
+    precision = _native_only(kwargs, "pobtasi")
+    lib = _lib.load()
+    device, w = _prepare((D, Lo, Ar, T, buffer),
+                         ("L_diagonal_blocks", "L_lower_diagonal_blocks", "L_lower_arrow_blocks",
+                          "L_arrow_tip_block", "buffer"))
+    _check_buffer(w[4].t, w[0].t)
+    m = _bta_struct(*(x.t for x in w[:4]))
+    with torch.cuda.device(device):
+        nbytes = ctypes.c_size_t(0)
+        _lib.raise_for(lib.sgb_pobtasi_permuted_workspace_size(ctypes.byref(m), precision, ctypes.byref(nbytes)),
+                       "pobtasi")
+        ws = _workspace(nbytes.value, device)
+        rc = lib.sgb_pobtasi_permuted(ctypes.byref(m), _ptr(w[4].t), precision, ws.data_ptr(), nbytes.value,
+                                      _stream(device))
+        _lib.raise_for(rc, "pobtasi")
+        _finish(w)
+
+
+def _pobtas_permuted(D, Lo, Ar, T, B, buffer, trans, kwargs):
+    """pobtas(..., buffer=): src/serinv/algs/pobtas.py:164-218."""
+    precision = _native_only(kwargs, "pobtas")
+    lib = _lib.load()
+    device, w = _prepare((D, Lo, Ar, T, B, buffer),
+                         ("L_diagonal_blocks", "L_lower_diagonal_blocks", "L_lower_arrow_blocks",
+                          "L_arrow_tip_block", "B", "buffer"))
+    _check_buffer(w[5].t, w[0].t)
+    m = _bta_struct(*(x.t for x in w[:4]))
+    Bt = w[4].t
+    if Bt.dim() == 1:
+        Bt = Bt.view(-1, 1)
+    N = m.n * m.b + m.a
+    if Bt.dim() != 2 or Bt.shape[0] != N:
+        raise ValueError(f"B must have shape ({N}, nrhs), got {tuple(w[4].t.shape)}")
+    if Bt.dtype != w[0].t.dtype:
+        raise TypeError(f"B has dtype {Bt.dtype}, the factor has {w[0].t.dtype}")
+    nrhs = Bt.shape[1]
+    with torch.cuda.device(device):
+        nbytes = ctypes.c_size_t(0)
+        _lib.raise_for(lib.sgb_pobtas_workspace_size(ctypes.byref(m), nrhs, precision, ctypes.byref(nbytes)),
+                       "pobtas")
+        ws = _workspace(nbytes.value, device)
+        rc = lib.sgb_pobtas_permuted(ctypes.byref(m), _ptr(w[5].t), _ptr(Bt), nrhs, max(nrhs, 1), trans.encode(),
+                                     precision, ws.data_ptr(), nbytes.value, _stream(device))
+        _lib.raise_for(rc, "pobtas")
+        _finish(w)
+
+
+# --------------------------------------------------------------------------
 # block tridiagonal (no arrowhead) family: the same kernels with a = 0
 
 
@@ -317,7 +418,7 @@ def pobtf(A_diagonal_blocks, A_lower_diagonal_blocks, **kwargs):
     """Cholesky factorization of a block tridiagonal SPD matrix, in place.
 
     Mirrors src/serinv/algs/pobtf.py:11-80 (kwargs ``device_streaming``,
-    ``buffer`` -- not supported yet, NotImplementedError --,
+    ``buffer`` -- the permuted form, _pobtf_permuted pobtf.py:125-185 --,
     ``factorize_last_block``; unknown keywords raise TypeError, pobtf.py:
     44-47).  Computes what pobtaf computes with an empty arrowhead.
     """
@@ -332,8 +433,9 @@ def pobtsi(L_diagonal_blocks, L_lower_diagonal_blocks, **kwargs):
     """Selected inversion of a block tridiagonal matrix from its Cholesky factor, in place.
 
     Mirrors src/serinv/algs/pobtsi.py:10-75 (kwargs ``device_streaming``,
-    ``buffer`` -- not supported yet --, ``invert_last_block``; unknown
-    keywords raise TypeError, pobtsi.py:39-42).
+    ``buffer`` -- _pobtsi_permuted, pobtsi.py:128-179 --,
+    ``invert_last_block``; unknown keywords raise TypeError, pobtsi.py:
+    39-42).
     """
     unexpected = set(kwargs) - _POBTASI_KW - _EXTENSION_KW
     if unexpected:
@@ -346,8 +448,13 @@ def pobts(L_diagonal_blocks, L_lower_diagonal_blocks, B, trans="N", **kwargs):
     """Triangular solve with the Cholesky factor of a block tridiagonal matrix, in place on ``B``.
 
     Mirrors src/serinv/algs/pobts.py:10-55 (``trans`` "N", "T" or "C";
-    ``partial``; ``device_streaming`` and ``buffer`` raise
-    NotImplementedError; unknown keywords are ignored, as there).
+    ``partial``; ``buffer`` -- _pobts_permuted, pobts.py:121-165 --;
+    ``device_streaming`` raises NotImplementedError; unknown keywords are
+    ignored, as there).
     """
+    if kwargs.get("device_streaming", False):
+        what = "Permuted arrowhead is not implemented." if kwargs.get("buffer", None) is not None else \
+            "Streaming is not implemented for the natural arrowhead."
+        raise NotImplementedError(what)
     Ar, T = _empty_arrow(L_diagonal_blocks)
     pobtas(L_diagonal_blocks, L_lower_diagonal_blocks, Ar, T, B, trans=trans, **kwargs)

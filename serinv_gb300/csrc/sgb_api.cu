@@ -694,6 +694,261 @@ int pobtas_native(const sgb_bta* m, T* Bm, int64_t nrhs, int64_t ldb, char trans
     return SGB_OK;
 }
 
+// ---- permuted (middle-partition) variants -------------------------------
+// The two-sided elimination of a middle partition with the fill-in column
+// `buf` (n, b, b): buf[i] holds the top block row's coupling to block i
+// (src/serinv/algs/pobtaf.py:186-281, pobtasi.py:175-244, pobtas.py:
+// 164-218).  Storage precision only (SIMT products, launch-based tile
+// sweep); the reduced system (blocks 0 and n-1, the tip) is the caller's.
+
+template <typename T>
+GemmProb<T> upd_prob(T* C, int64_t ldc, int64_t M, int64_t N, T alpha, T beta) {
+    GemmProb<T> p = prob<T>();
+    p.M = (int32_t)M;
+    p.N = (int32_t)N;
+    p.alpha = alpha;
+    p.beta = beta;
+    if (beta != T(0)) {
+        p.Cin = C;
+        p.ldcin = ldc;
+    }
+    p.Cout = C;
+    p.ldc = ldc;
+    return p;
+}
+
+template <typename T>
+int pobtaf_permuted_run(const sgb_bta* m, T* buf, void* ws, int32_t* info, cudaStream_t s) {
+    const int64_t n = m->n, b = m->b, a = m->a;
+    T* D = (T*)m->diag;
+    T* Lo = (T*)m->lower;
+    T* Ar = (T*)m->arrow;
+    T* Tp = (T*)m->tip;
+    PobtafWs<T> L(m, 0);
+    T* tinv = (T*)((char*)ws + L.tinv);
+    const int64_t bb = b * b, ab = a * b;
+    {   // buf[1] = Lo[0]^T  (pobtaf.py:203)
+        GemmProb<T> c = copy_prob<T>(buf + bb, b, Lo, b, b, b);
+        c.transCin = 1;
+        SGB_TRY(gemm_simt<T>(&c, 1, s));
+    }
+    for (int64_t i = 1; i < n - 1; ++i) {  // :206
+        // [D_i; Lo_i; buf_i; Ar_i] <- Cholesky of the column block  (:208-242)
+        RowSet<T> r1{Lo + i * bb, b, b}, r2{buf + i * bb, b, b}, r3{a ? Ar + i * ab : nullptr, a, b};
+        cudaError_t e = factor_column_block<T>(D + i * bb, b, b, r1, r2, tinv, info, i * b, s, r3);
+        if (e != cudaSuccess) return cuda_fail(e);
+        GemmProb<T> pr[6];
+        int np = 0;
+        const T* lo = Lo + i * bb;
+        const T* bu = buf + i * bb;
+        const T* ar = Ar + i * ab;
+        GemmProb<T> p = upd_prob<T>(D + (i + 1) * bb, b, b, b, T(-1), T(1));  // :246-250
+        set_term<T>(p, 0, lo, b, 0, lo, b, 1, b);
+        pr[np++] = p;
+        p = upd_prob<T>(D, b, b, b, T(-1), T(1));  // D_0 -= buf_i buf_i^T  (:267-269)
+        set_term<T>(p, 0, bu, b, 0, bu, b, 1, b);
+        pr[np++] = p;
+        p = upd_prob<T>(buf + (i + 1) * bb, b, b, b, T(-1), T(0));  // buf_{i+1} = -buf_i Lo_i^T  (:272-274)
+        set_term<T>(p, 0, bu, b, 0, lo, b, 1, b);
+        pr[np++] = p;
+        if (a) {
+            p = upd_prob<T>(Ar + (i + 1) * ab, b, a, b, T(-1), T(1));  // :253-256
+            set_term<T>(p, 0, ar, b, 0, lo, b, 1, b);
+            pr[np++] = p;
+            p = upd_prob<T>(Tp, a, a, a, T(-1), T(1));  // :260-263
+            set_term<T>(p, 0, ar, b, 0, ar, b, 1, b);
+            pr[np++] = p;
+            p = upd_prob<T>(Ar, b, a, b, T(-1), T(1));  // Ar_0 -= Ar_i buf_i^T  (:278-281)
+            set_term<T>(p, 0, ar, b, 0, bu, b, 1, b);
+            pr[np++] = p;
+        }
+        SGB_TRY(gemm_simt<T>(pr, np, s));
+    }
+    return SGB_OK;
+}
+
+// pobtasi_permuted scratch: per chunk of blocks L_ii^{-1}, G_i = Lo_i L_ii^{-1},
+// F_i = buf_i L_ii^{-1}, H_i = Ar_i L_ii^{-1}, and the inversion scratch.
+template <typename T>
+struct PobtasiPermWs {
+    size_t status, linv, trtri, gfh, total;
+    int64_t chunk;
+    explicit PobtasiPermWs(const sgb_bta* m) {
+        const int64_t n = m->n, b = m->b, a = m->a;
+        chunk = n < kSiChunk ? (n > 0 ? n : 1) : kSiChunk;
+        Carve c;
+        status = c.take(256);
+        linv = c.take(sizeof(T) * (size_t)(chunk * b * b));
+        trtri = c.take(sizeof(T) * trtri_scratch_elems(b, chunk));
+        gfh = c.take(sizeof(T) * (size_t)(chunk * (2 * b + a) * b));
+        total = c.off;
+    }
+};
+
+template <typename T>
+int pobtasi_permuted_run(const sgb_bta* m, T* buf, void* ws, cudaStream_t s) {
+    const int64_t n = m->n, b = m->b, a = m->a;
+    T* D = (T*)m->diag;
+    T* Lo = (T*)m->lower;
+    T* Ar = (T*)m->arrow;
+    T* Tp = (T*)m->tip;
+    PobtasiPermWs<T> W(m);
+    char* base = (char*)ws;
+    T* Linv = (T*)(base + W.linv);
+    T* trs = (T*)(base + W.trtri);
+    T* GFH = (T*)(base + W.gfh);
+    const int64_t bb = b * b, ab = a * b, gs = (2 * b + a) * b;
+    Ctx native;
+    // blocks n-2 .. 1, in chunks from the bottom (pobtasi.py:199)
+    for (int64_t hi = n - 1; hi > 1; hi -= W.chunk) {
+        const int64_t lo = hi - W.chunk > 1 ? hi - W.chunk : 1;
+        const int64_t cnt = hi - lo;
+        SGB_TRY(trtri_run<T>(native, D + lo * bb, b, cnt, Linv, trs, s));
+        // G, F, H from the factor, P = L^{-T} L^{-1} into D_j (L_jj is dead then)
+        GemmProb<T> pr[4];
+        int np = 0;
+        GemmProb<T> p = prob<T>();
+        p.M = p.N = (int32_t)b;
+        p.batch = (int32_t)cnt;
+        set_term<T>(p, 0, Lo + lo * bb, b, 0, Linv, b, 0, b, KM_GE_N0);
+        p.term[0].strideA = bb;
+        p.term[0].strideB = bb;
+        p.Cout = GFH;
+        p.ldc = b;
+        p.strideC = gs;
+        pr[np++] = p;
+        GemmProb<T> q = p;
+        q.term[0].A = buf + lo * bb;
+        q.Cout = GFH + bb;
+        pr[np++] = q;
+        if (a) {
+            GemmProb<T> h = prob<T>();
+            h.M = (int32_t)a;
+            h.N = (int32_t)b;
+            h.batch = (int32_t)cnt;
+            set_term<T>(h, 0, Ar + lo * ab, b, 0, Linv, b, 0, b, KM_GE_N0);
+            h.term[0].strideA = ab;
+            h.term[0].strideB = bb;
+            h.Cout = GFH + 2 * bb;
+            h.ldc = b;
+            h.strideC = gs;
+            pr[np++] = h;
+        }
+        GemmProb<T> pp = prob<T>();
+        pp.M = pp.N = (int32_t)b;
+        pp.batch = (int32_t)cnt;
+        set_term<T>(pp, 0, Linv, b, 1, Linv, b, 0, b, KM_GE_M0);
+        pp.term[0].strideA = bb;
+        pp.term[0].strideB = bb;
+        pp.Cout = D + lo * bb;
+        pp.ldc = b;
+        pp.strideC = bb;
+        pr[np++] = pp;
+        SGB_TRY(gemm_simt<T>(pr, np, s));
+        for (int64_t i = hi - 1; i >= lo; --i) {
+            const T* G = GFH + (i - lo) * gs;
+            const T* F = G + bb;
+            const T* H = G + 2 * bb;
+            GemmProb<T> x[3];
+            // X_{i+1,i} = -(X_{top,i+1}^T F + X_{i+1,i+1} G + X_{A,i+1}^T H)  (:211-216)
+            x[0] = upd_prob<T>(Lo + i * bb, b, b, b, T(-1), T(0));
+            set_term<T>(x[0], 0, buf + (i + 1) * bb, b, 1, F, b, 0, b);
+            set_term<T>(x[0], 1, D + (i + 1) * bb, b, 0, G, b, 0, b);
+            if (a) set_term<T>(x[0], 2, Ar + (i + 1) * ab, b, 1, H, b, 0, a);
+            // X_{top,i} = -(X_{top,i+1} G + X_{top,top} F + X_{A,top}^T H)  (:219-223)
+            x[1] = upd_prob<T>(buf + i * bb, b, b, b, T(-1), T(0));
+            set_term<T>(x[1], 0, buf + (i + 1) * bb, b, 0, G, b, 0, b);
+            set_term<T>(x[1], 1, D, b, 0, F, b, 0, b);
+            if (a) set_term<T>(x[1], 2, Ar, b, 1, H, b, 0, a);
+            int nx = 2;
+            if (a) {  // X_{A,i} = -(X_{A,i+1} G + X_{A,top} F + X_T H)  (:227-231)
+                x[2] = upd_prob<T>(Ar + i * ab, b, a, b, T(-1), T(0));
+                set_term<T>(x[2], 0, Ar + (i + 1) * ab, b, 0, G, b, 0, b);
+                set_term<T>(x[2], 1, Ar, b, 0, F, b, 0, b);
+                set_term<T>(x[2], 2, Tp, a, 0, H, b, 0, a);
+                nx = 3;
+            }
+            SGB_TRY(gemm_simt<T>(x, nx, s));
+            // X_ii = P_i - X_{i+1,i}^T G - X_{top,i}^T F - X_{A,i}^T H  (:234-241)
+            GemmProb<T> d = upd_prob<T>(D + i * bb, b, b, b, T(-1), T(1));
+            set_term<T>(d, 0, Lo + i * bb, b, 1, G, b, 0, b);
+            set_term<T>(d, 1, buf + i * bb, b, 1, F, b, 0, b);
+            if (a) set_term<T>(d, 2, Ar + i * ab, b, 1, H, b, 0, a);
+            SGB_TRY(gemm_simt<T>(&d, 1, s));
+        }
+    }
+    // X_{1,0} = X_{top,1}^T  (:244)
+    GemmProb<T> c = copy_prob<T>(Lo, b, buf + bb, b, b, b);
+    c.transCin = 1;
+    SGB_TRY(gemm_simt<T>(&c, 1, s));
+    return SGB_OK;
+}
+
+template <typename T>
+int pobtas_permuted_run(const sgb_bta* m, T* buf, T* Bm, int64_t nrhs, int64_t ldb, char trans, void* ws,
+                        cudaStream_t s) {
+    const int64_t n = m->n, b = m->b, a = m->a;
+    T* D = (T*)m->diag;
+    T* Lo = (T*)m->lower;
+    T* Ar = (T*)m->arrow;
+    PobtasWs<T> W(m, nrhs);
+    char* base = (char*)ws;
+    T* Linv = (T*)(base + W.linv);
+    T* trs = (T*)(base + W.trtri);
+    T* y = (T*)(base + W.y);
+    const int64_t bb = b * b, ab = a * b;
+    T* Btip = Bm + n * b * ldb;
+    auto Bi = [&](int64_t i) { return Bm + i * b * ldb; };
+    if (nrhs == 0 || n < 3) return SGB_OK;
+    Ctx native;
+    SGB_TRY(trtri_run<T>(native, D + bb, b, n - 2, Linv, trs, s));  // blocks 1 .. n-2
+    auto Li = [&](int64_t i) { return Linv + (i - 1) * bb; };
+    if (trans == 'N') {  // pobtas.py:179-203
+        for (int64_t i = 1; i < n - 1; ++i) {
+            GemmProb<T> p = prob<T>();  // y = L_ii^{-1} B_i
+            p.M = (int32_t)b;
+            p.N = (int32_t)nrhs;
+            set_term<T>(p, 0, Li(i), b, 0, Bi(i), ldb, 0, b, KM_LT_M1);
+            p.Cout = y;
+            p.ldc = nrhs;
+            SGB_TRY(gemm_simt<T>(&p, 1, s));
+            GemmProb<T> pr[4];
+            int np = 0;
+            pr[np++] = copy_prob<T>(Bi(i), ldb, y, nrhs, b, nrhs);
+            GemmProb<T> q = upd_prob<T>(Bi(i + 1), ldb, b, nrhs, T(-1), T(1));
+            set_term<T>(q, 0, Lo + i * bb, b, 0, y, nrhs, 0, b);
+            pr[np++] = q;
+            q = upd_prob<T>(Bi(0), ldb, b, nrhs, T(-1), T(1));
+            set_term<T>(q, 0, buf + i * bb, b, 0, y, nrhs, 0, b);
+            pr[np++] = q;
+            if (a) {
+                q = upd_prob<T>(Btip, ldb, a, nrhs, T(-1), T(1));
+                set_term<T>(q, 0, Ar + i * ab, b, 0, y, nrhs, 0, b);
+                pr[np++] = q;
+            }
+            SGB_TRY(gemm_simt<T>(pr, np, s));
+        }
+        return SGB_OK;
+    }
+    for (int64_t i = n - 2; i >= 1; --i) {  // pobtas.py:204-216
+        GemmProb<T> p = upd_prob<T>(Bi(i), ldb, b, nrhs, T(-1), T(1));
+        set_term<T>(p, 0, Lo + i * bb, b, 1, Bi(i + 1), ldb, 0, b);
+        set_term<T>(p, 1, buf + i * bb, b, 1, Bi(0), ldb, 0, b);
+        if (a) set_term<T>(p, 2, Ar + i * ab, b, 1, Btip, ldb, 0, a);
+        SGB_TRY(gemm_simt<T>(&p, 1, s));
+        GemmProb<T> q = prob<T>();  // y = L_ii^{-T} B_i
+        q.M = (int32_t)b;
+        q.N = (int32_t)nrhs;
+        set_term<T>(q, 0, Li(i), b, 1, Bi(i), ldb, 0, b, KM_GE_M0);
+        q.Cout = y;
+        q.ldc = nrhs;
+        SGB_TRY(gemm_simt<T>(&q, 1, s));
+        GemmProb<T> c = copy_prob<T>(Bi(i), ldb, y, nrhs, b, nrhs);
+        SGB_TRY(gemm_simt<T>(&c, 1, s));
+    }
+    return SGB_OK;
+}
+
 }  // namespace
 }  // namespace sgb
 
@@ -859,6 +1114,71 @@ int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char tran
     if (m->dtype == SGB_F64)
         return pobtas_native<double>(m, (double*)rhs, nrhs, ldb, trans, partial, workspace, s);
     return pobtas_native<float>(m, (float*)rhs, nrhs, ldb, trans, partial, workspace, s);
+}
+
+int sgb_pobtaf_permuted(const sgb_bta* m, void* buffer, int precision, void* workspace, size_t workspace_bytes,
+                        int32_t* info, void* stream) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
+    if (S != 0) return SGB_ERR_UNSUPPORTED;
+    if (m->n < 2) return SGB_ERR_SHAPE;
+    if (buffer == nullptr) return SGB_ERR_ARG;
+    size_t need = 0;
+    sgb_pobtaf_workspace_size(m, precision, &need);
+    if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
+    if (m->dtype == SGB_F64) return pobtaf_permuted_run<double>(m, (double*)buffer, workspace, info, s);
+    return pobtaf_permuted_run<float>(m, (float*)buffer, workspace, info, s);
+}
+
+int sgb_pobtasi_permuted_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
+    if (S != 0) return SGB_ERR_UNSUPPORTED;
+    if (!bytes) return SGB_ERR_ARG;
+    *bytes = m->dtype == SGB_F64 ? PobtasiPermWs<double>(m).total : PobtasiPermWs<float>(m).total;
+    return SGB_OK;
+}
+
+int sgb_pobtasi_permuted(const sgb_bta* m, void* buffer, int precision, void* workspace, size_t workspace_bytes,
+                         void* stream) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
+    if (S != 0) return SGB_ERR_UNSUPPORTED;
+    if (m->n < 2) return SGB_ERR_SHAPE;
+    if (buffer == nullptr) return SGB_ERR_ARG;
+    size_t need = 0;
+    sgb_pobtasi_permuted_workspace_size(m, precision, &need);
+    if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (m->dtype == SGB_F64) return pobtasi_permuted_run<double>(m, (double*)buffer, workspace, s);
+    return pobtasi_permuted_run<float>(m, (float*)buffer, workspace, s);
+}
+
+int sgb_pobtas_permuted(const sgb_bta* m, void* buffer, void* rhs, int64_t nrhs, int64_t ldb, char trans,
+                        int precision, void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = check_bta(m);
+    if (rc) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    if (S < 0) return -S;
+    if (S != 0) return SGB_ERR_UNSUPPORTED;
+    if (trans != 'N' && trans != 'T' && trans != 'C') return SGB_ERR_ARG;
+    if (nrhs < 0 || nrhs > (1 << 20) || ldb < nrhs) return SGB_ERR_SHAPE;
+    if ((nrhs > 0 && rhs == nullptr) || buffer == nullptr) return SGB_ERR_ARG;
+    size_t need = 0;
+    sgb_pobtas_workspace_size(m, nrhs, precision, &need);
+    if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (m->dtype == SGB_F64)
+        return pobtas_permuted_run<double>(m, (double*)buffer, (double*)rhs, nrhs, ldb, trans, workspace, s);
+    return pobtas_permuted_run<float>(m, (float*)buffer, (float*)rhs, nrhs, ldb, trans, workspace, s);
 }
 
 }  // extern "C"

@@ -850,6 +850,8 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
                     cudaStream_t s) {
     if (np > kMaxTcProbs) return cudaErrorInvalidValue;
     if (S != 3 && S != 4 && S != 5 && S != 6 && S != 7) return cudaErrorInvalidValue;
+    for (int i = 0; i < np; ++i)
+        if (probs[i].nterms > 2) return cudaErrorInvalidValue;  // two sources per split job
     SplitLaunch SL;
     memset(&SL, 0, sizeof(SL));
     SL.S = S;

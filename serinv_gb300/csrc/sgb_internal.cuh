@@ -39,9 +39,12 @@ struct GemmTerm {
 // instances.  Cin may alias Cout when transCin == 0 (each element is read
 // and written by the same thread).  A term operand may alias Cout only when
 // N <= the tile width (one tile column, rows owned by one CTA).
+// Up to three terms per problem (the tensor-core path takes at most two).
+constexpr int kMaxTerms = 3;
+
 template <typename T>
 struct GemmProb {
-    GemmTerm<T> term[2];
+    GemmTerm<T> term[kMaxTerms];
     const T* Cin;
     T* Cout;
     int64_t ldcin, ldc;
@@ -85,7 +88,7 @@ cudaError_t trtri_tiles_batched(const T* L, int64_t ldl, int64_t strideL, int m,
                                 T* Linv, int64_t ldx, int64_t strideX, cudaStream_t s);
 
 // Blocked in-place Cholesky of the column block [diag; rows_1; ...; rows_k]
-// (the diagonal block m x m and up to two row sets with m columns), i.e.
+// (the diagonal block m x m and up to three row sets with m columns), i.e.
 // diag <- chol(diag), rows_j <- rows_j * L^{-T}.  Scratch: kTile*kTile T.
 template <typename T>
 struct RowSet {
@@ -95,7 +98,8 @@ struct RowSet {
 
 template <typename T>
 cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, RowSet<T> r2,
-                                T* scratch, int32_t* info, int64_t info_row0, cudaStream_t s);
+                                T* scratch, int32_t* info, int64_t info_row0, cudaStream_t s,
+                                RowSet<T> r3 = RowSet<T>{nullptr, 0, 0});
 
 // A grouped-product engine: the SIMT kernel, or a context-bound dispatcher
 // that sends products to the tensor cores.

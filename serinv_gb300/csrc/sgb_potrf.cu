@@ -90,7 +90,7 @@ cudaError_t trtri_tiles_batched(const T* L, int64_t ldl, int64_t strideL, int m,
 
 template <typename T>
 cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, RowSet<T> r2, T* scratch,
-                                int32_t* info, int64_t info_row0, cudaStream_t s) {
+                                int32_t* info, int64_t info_row0, cudaStream_t s, RowSet<T> r3) {
     cudaError_t err;
     for (int64_t c0 = 0; c0 < m; c0 += kTile) {
         const int w = (int)((m - c0) < kTile ? (m - c0) : kTile);
@@ -100,7 +100,7 @@ cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, R
         if (err != cudaSuccess) return err;
 
         // rows below the tile: P[:, c0:c1] <- P[:, c0:c1] * Ltile^{-T}
-        GemmProb<T> pr[3];
+        GemmProb<T> pr[4];
         int np = 0;
         auto trsm = [&](T* base, int64_t rows, int64_t ld) {
             if (rows <= 0) return;
@@ -122,6 +122,7 @@ cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, R
         trsm(diag + c1 * ldd, right, ldd);
         trsm(r1.p, r1.rows, r1.ld);
         trsm(r2.p, r2.rows, r2.ld);
+        trsm(r3.p, r3.rows, r3.ld);
         if (np) {
             err = gemm_simt<T>(pr, np, s);
             if (err != cudaSuccess) return err;
@@ -155,6 +156,7 @@ cudaError_t factor_column_block(T* diag, int64_t m, int64_t ldd, RowSet<T> r1, R
         upd(diag + c1 * ldd, right, ldd, 1);
         upd(r1.p, r1.rows, r1.ld, 0);
         upd(r2.p, r2.rows, r2.ld, 0);
+        upd(r3.p, r3.rows, r3.ld, 0);
         err = gemm_simt<T>(pr, np, s);
         if (err != cudaSuccess) return err;
     }
@@ -242,7 +244,7 @@ cudaError_t trtri_batched(const T* L, int64_t ldl, int64_t strideL, int64_t m, i
     template cudaError_t trtri_tiles_batched<T>(const T*, int64_t, int64_t, int, int, T*, int64_t,       \
                                                 int64_t, cudaStream_t);                                   \
     template cudaError_t factor_column_block<T>(T*, int64_t, int64_t, RowSet<T>, RowSet<T>, T*,          \
-                                                int32_t*, int64_t, cudaStream_t);                         \
+                                                int32_t*, int64_t, cudaStream_t, RowSet<T>);              \
     template cudaError_t trtri_batched<T>(const T*, int64_t, int64_t, int64_t, int64_t, T*, int64_t,     \
                                           int64_t, T*, cudaStream_t, GemmFn<T>, void*);
 SGB_INST(double)

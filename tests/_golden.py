@@ -26,6 +26,20 @@ def all_full_cases():
     return load_cases("reference_suite_grid.npz") + load_cases("synthetic_small.npz")
 
 
+def permuted_cases():
+    """(key, inputs, after permuted pobtaf, final selected inverse, final solution)
+    for the middle-partition workflow cases (make_golden.py, permuted_cases)."""
+    z = np.load(os.path.join(GOLDEN, "permuted.npz"))
+    out = []
+    for key in z["cases"]:
+        key = str(key)
+        inp = {k: z[f"{key}in_{k}"] for k in ("D", "Lo", "Ar", "T", "B")}
+        F = {k: z[f"{key}F_{k}"] for k in ("D", "Lo", "Ar", "T", "buf")}
+        X = {k: z[f"{key}X_{k}"] for k in ("D", "Lo", "Ar", "T", "buf")}
+        out.append((key, inp, F, X, z[f"{key}x"]))
+    return out
+
+
 def bench_digest():
     return dict(np.load(os.path.join(GOLDEN, "bench_n128_b64_a16.npz")))
 

@@ -13,9 +13,12 @@ arrow width 0, ``pobtf`` / ``pobtsi`` / ``pobts``), runs them on
 * the seeded synthetic generator of this repository at small and at the
   CPU-runnable benchmark shape (n=128, b=64, a=16, 1 RHS),
 
-and stores inputs and outputs (full arrays for small cases, a digest plus
-edge blocks for the 128x64 case) as compressed ``.npz`` files beside this
-script, with the NumPy/SciPy versions in ``versions.json``.
+and the permuted middle-partition workflow (``buffer=``, as the
+reference's permuted tests drive it) on small synthetic inputs, and stores
+inputs and outputs (full arrays for small cases, a digest plus edge blocks
+for the 128x64 case) as compressed ``.npz`` files beside this script, with
+the NumPy/SciPy versions in ``versions.json``.  ``--only=permuted`` writes
+the permuted file alone.
 """
 
 from __future__ import annotations
@@ -81,9 +84,77 @@ def _pack(prefix, D, Lo, Ar, T, B, L, X, x):
     return out
 
 
-def main(ref_root: str) -> None:
+def _reduced(D, Ar, T, buf):
+    """The reduced system of a middle partition (blocks 0 and n-1, the tip),
+    as the reference's permuted tests build it
+    (tests/tests_algs/permuted/test_bta/test_pobtasi_permuted.py:94-115)."""
+    b, a = D.shape[1], Ar.shape[1]
+    rD = np.zeros((2, b, b), dtype=D.dtype)
+    rLo = np.zeros((1, b, b), dtype=D.dtype)
+    rAr = np.zeros((2, a, b), dtype=D.dtype)
+    rD[0], rD[1] = D[0], D[-1]
+    rLo[0] = buf[-1].conj().T
+    rAr[0], rAr[1] = Ar[0], Ar[-1]
+    return rD, rLo, rAr, T.copy()
+
+
+def _map_back(D, Ar, T, buf, rD, rLo, rAr, rT):
+    D[0], D[-1] = rD[0], rD[1]
+    buf[-1] = rLo[0].conj().T
+    Ar[0], Ar[-1] = rAr[0], rAr[1]
+    T[:, :] = rT
+
+
+def permuted_cases(ref, generate):
+    """The middle-partition workflow of the reference's permuted tests:
+    permuted pobtaf -> reduced system (pobtaf, then pobtasi or pobtas) ->
+    permuted pobtasi / permuted pobtas N and C, on seeded synthetic inputs."""
+    out = {}
+    cases = []
+    for (n, b, a, nrhs, seed) in [(3, 5, 3, 2, 11), (4, 16, 4, 3, 12), (6, 40, 7, 2, 13), (5, 33, 1, 1, 14)]:
+        m = generate(n, b, a, nrhs, seed=seed)
+        D, Lo, Ar, T, B = (x.copy() for x in (m.D, m.Lo, m.Ar, m.T, m.B))
+        buf = np.zeros_like(D)
+        ref["pobtaf"](D, Lo, Ar, T, buffer=buf)
+        F = [x.copy() for x in (D, Lo, Ar, T, buf)]
+        rD, rLo, rAr, rT = _reduced(D, Ar, T, buf)
+        ref["pobtaf"](rD, rLo, rAr, rT)
+        rL = [x.copy() for x in (rD, rLo, rAr, rT)]
+        # selected inversion
+        XD, XLo, XAr, XT, Xbuf = (x.copy() for x in (D, Lo, Ar, T, buf))
+        sD, sLo, sAr, sT = (x.copy() for x in rL)
+        ref["pobtasi"](sD, sLo, sAr, sT)
+        _map_back(XD, XAr, XT, Xbuf, sD, sLo, sAr, sT)
+        ref["pobtasi"](XD, XLo, XAr, XT, buffer=Xbuf)
+        # solve
+        LD, LLo, LAr, LT, Lbuf = (x.copy() for x in (D, Lo, Ar, T, buf))
+        _map_back(LD, LAr, LT, Lbuf, *rL)
+        x = B.copy()
+        ref["pobtas"](LD, LLo, LAr, LT, x, buffer=Lbuf, trans="N")
+        rB = np.concatenate([x[:b], x[(n - 1) * b:n * b], x[n * b:]])
+        ref["pobtas"](*rL, rB, trans="N")
+        ref["pobtas"](*rL, rB, trans="C")
+        x[:b], x[(n - 1) * b:n * b], x[n * b:] = rB[:b], rB[b:2 * b], rB[2 * b:]
+        ref["pobtas"](LD, LLo, LAr, LT, x, buffer=Lbuf, trans="C")
+        key = f"n{n}_b{b}_a{a}_r{nrhs}_s{seed}_"
+        for name, arr in zip(("D", "Lo", "Ar", "T", "B"), (m.D, m.Lo, m.Ar, m.T, m.B)):
+            out[f"{key}in_{name}"] = arr
+        for name, arr in zip(("D", "Lo", "Ar", "T", "buf"), F):
+            out[f"{key}F_{name}"] = arr
+        for name, arr in zip(("D", "Lo", "Ar", "T", "buf"), (XD, XLo, XAr, XT, Xbuf)):
+            out[f"{key}X_{name}"] = arr
+        out[f"{key}x"] = x
+        cases.append(key)
+    out["cases"] = np.array(cases)
+    np.savez_compressed(os.path.join(HERE, "permuted.npz"), **out)
+
+
+def main(ref_root: str, only: str | None = None) -> None:
     ref, tu = _load_reference(ref_root)
     from serinv_gb300.synthetic import generate
+    if only == "permuted":
+        permuted_cases(ref, generate)
+        return
 
     # 1) The reference test suite's own input family and parameter grid.
     suite = {}
@@ -139,6 +210,9 @@ def main(ref_root: str) -> None:
         dig[f"{tag}_T"] = stacks[3]
     np.savez_compressed(os.path.join(HERE, "bench_n128_b64_a16.npz"), **dig)
 
+    # 4) The permuted (middle-partition) variants.
+    permuted_cases(ref, generate)
+
     import scipy
     with open(os.path.join(HERE, "versions.json"), "w") as f:
         json.dump({"numpy": np.__version__, "scipy": scipy.__version__,
@@ -147,4 +221,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [x for x in sys.argv[1:] if not x.startswith("--only=")]
+    only = next((x.split("=", 1)[1] for x in sys.argv[1:] if x.startswith("--only=")), None)
+    main(args[0] if args else "/root/reference", only)

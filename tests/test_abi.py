@@ -91,6 +91,29 @@ def test_null_and_workspace_errors(lib):
     assert lib.sgb_pobtaf(ctypes.byref(m), 1, 9, 0x1000, 1 << 20, None, None) == _lib.SGB_ERR_ARG
 
 
+def test_permuted_entry_points_host_checks(lib):
+    """The buffer= entry points validate on the host before any launch."""
+    m = _desc(n=4, b=8, a=2)
+    sz = ctypes.c_size_t(0)
+    assert lib.sgb_pobtasi_permuted_workspace_size(ctypes.byref(m), 0, ctypes.byref(sz)) == 0
+    assert sz.value % 256 == 0 and sz.value >= 4 * 8 * 8 * 8
+    mixed = _lib.SGB_PREC_MIXED
+    assert lib.sgb_pobtasi_permuted_workspace_size(ctypes.byref(m), mixed, ctypes.byref(sz)) == \
+        _lib.SGB_ERR_UNSUPPORTED
+    assert lib.sgb_pobtaf_permuted(ctypes.byref(m), 0x1000, mixed, 0x1000, 1 << 30, None, None) == \
+        _lib.SGB_ERR_UNSUPPORTED
+    assert lib.sgb_pobtaf_permuted(ctypes.byref(m), None, 0, 0x1000, 1 << 30, None, None) == _lib.SGB_ERR_ARG
+    assert lib.sgb_pobtaf_permuted(ctypes.byref(m), 0x1000, 0, None, 0, None, None) == _lib.SGB_ERR_WORKSPACE
+    assert lib.sgb_pobtasi_permuted(ctypes.byref(m), 0x1000, 0, 0x1000, 8, None) == _lib.SGB_ERR_WORKSPACE
+    assert lib.sgb_pobtas_permuted(ctypes.byref(m), 0x1000, 0x1000, 2, 2, b"X", 0, 0x1000, 1 << 30, None) == \
+        _lib.SGB_ERR_ARG
+    assert lib.sgb_pobtas_permuted(ctypes.byref(m), 0x1000, 0x1000, 2, 1, b"N", 0, 0x1000, 1 << 30, None) == \
+        _lib.SGB_ERR_SHAPE
+    one = _desc(n=1, b=8, a=2)
+    assert lib.sgb_pobtaf_permuted(ctypes.byref(one), 0x1000, 0, 0x1000, 1 << 30, None, None) == \
+        _lib.SGB_ERR_SHAPE
+
+
 def test_error_mapping():
     with pytest.raises(ValueError):
         _lib.raise_for(_lib.SGB_ERR_SHAPE, "x")

@@ -35,14 +35,37 @@ def test_pobtas_streaming_not_implemented(m):
         sg.pobtas(*m.arrays(), m.B, device_streaming=True)
 
 
-def test_permuted_buffer_not_implemented(m):
+def test_permuted_mixed_precision_not_implemented(m):
+    """buffer= computes in the storage precision; the slice products are not offered there."""
     buf = np.empty_like(m.D)
     with pytest.raises(NotImplementedError):
+        sg.pobtaf(*m.arrays(), buffer=buf, precision="mixed")
+    with pytest.raises(NotImplementedError):
+        sg.pobtasi(*m.arrays(), buffer=buf, precision="mixed")
+    with pytest.raises(NotImplementedError):
+        sg.pobtas(*m.arrays(), m.B, buffer=buf, precision="mixed")
+
+
+def test_permuted_streaming_solve_not_implemented(m):
+    """pobtas.py:31-36 and pobts.py:29-32: streaming is refused for the permuted solve."""
+    buf = np.empty_like(m.D)
+    with pytest.raises(NotImplementedError, match="permuted"):
+        sg.pobtas(*m.arrays(), m.B, buffer=buf, device_streaming=True)
+    with pytest.raises(NotImplementedError, match="Permuted"):
+        sg.pobts(m.D, m.Lo, m.B[:m.D.shape[0] * m.D.shape[1]], buffer=buf, device_streaming=True)
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU behaviour")
+def test_permuted_no_gpu_fails_loudly(m):
+    buf = np.zeros_like(m.D)
+    before = m.D.copy()
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
         sg.pobtaf(*m.arrays(), buffer=buf)
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
         sg.pobtasi(*m.arrays(), buffer=buf)
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
         sg.pobtas(*m.arrays(), m.B, buffer=buf)
+    np.testing.assert_array_equal(m.D, before)
 
 
 def test_bad_precision(m):

@@ -119,3 +119,45 @@ def test_flop_counts():
     assert abs(f["pobtaf"] / 1e9 - 187.2) < 0.1
     assert abs(f["pobtasi"] / 1e9 - 497.5) < 0.1
     assert abs(f["pobtas"] / 1e9 - 13.9) < 0.1
+
+
+from _golden import permuted_cases  # noqa: E402
+from _permuted import workflow  # noqa: E402
+
+PERM = permuted_cases()
+
+
+def _oracle_fn():
+    return dict(pobtaf=oracle.pobtaf, pobtasi=oracle.pobtasi,
+                pobtas=lambda D, Lo, Ar, T, B, tr: oracle.pobtas(D, Lo, Ar, T, B, trans=tr),
+                pobtaf_p=oracle.pobtaf_permuted, pobtasi_p=oracle.pobtasi_permuted,
+                pobtas_p=lambda D, Lo, Ar, T, buf, B, tr: oracle.pobtas_permuted(D, Lo, Ar, T, B, buf, trans=tr))
+
+
+@pytest.mark.parametrize("case", PERM, ids=[c[0] for c in PERM])
+def test_oracle_permuted_matches_reference(case):
+    """The permuted restatements, driven through the middle-partition
+    workflow, reproduce the reference's own outputs."""
+    key, inp, F, X, x = case
+    D, Lo, Ar, T, B = (inp[k].copy() for k in ("D", "Lo", "Ar", "T", "B"))
+    Fo, Xo, xo = workflow(_oracle_fn(), D, Lo, Ar, T, B,
+                          zeros=lambda shape, ref: np.zeros(shape, dtype=ref.dtype), copy=lambda v: v.copy())
+    for got, name in zip(Fo, ("D", "Lo", "Ar", "T")):
+        assert rel_err(got, F[name]) <= 1e-14, ("F", name)
+    assert rel_err(Fo[4][1:], F["buf"][1:]) <= 1e-14
+    for got, name in zip(Xo, ("D", "Lo", "Ar", "T")):
+        assert rel_err(got, X[name]) <= 1e-14, ("X", name)
+    assert rel_err(xo, x) <= 1e-14
+
+
+@pytest.mark.parametrize("case", PERM, ids=[c[0] for c in PERM])
+def test_permuted_workflow_is_the_inverse(case):
+    """The golden workflow's results are A^{-1} on the BTA pattern and A^{-1} B."""
+    key, inp, F, X, x = case
+    A = oracle.bta_to_dense(inp["D"], inp["Lo"], inp["Ar"], inp["T"])
+    n, b, a = inp["D"].shape[0], inp["D"].shape[1], inp["Ar"].shape[1]
+    Ainv = np.linalg.inv(A)
+    D, Lo, Ar, T = oracle.dense_to_bta(Ainv, n, b, a)
+    for got, ref in ((X["D"], D), (X["Lo"], Lo), (X["Ar"], Ar), (X["T"], T)):
+        assert rel_err(got, ref) <= 1e-10
+    assert rel_err(x, np.linalg.solve(A, inp["B"])) <= 1e-10
