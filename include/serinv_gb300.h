@@ -51,6 +51,15 @@ extern "C" {
 /* ---- element types -------------------------------------------------- */
 #define SGB_F32 0
 #define SGB_F64 1
+/* Hermitian positive-definite complex matrices (interleaved re, im pairs,
+ * the layout of C99 complex / std::complex / NumPy complex arrays).  They
+ * run through the real embedding z = x + iy -> [x -y; y x]: the workspace
+ * holds the embedded stacks (twice the matrix's bytes) and the real sweeps
+ * run on blocks 2b and arrow 2a.  The imaginary part of the diagonal of the
+ * diagonal blocks and of the tip is ignored (taken as 0).  Info rows are
+ * complex rows.  SGB_C128 accepts SGB_PREC_MIXED (FP64 embedding). */
+#define SGB_C64  2
+#define SGB_C128 3
 
 /* ---- precision modes ------------------------------------------------ */
 /* Arithmetic in the storage type throughout: the drop-in form. */
@@ -68,7 +77,7 @@ extern "C" {
 #define SGB_PREC_MIXED  1
 
 typedef struct sgb_bta {
-    int32_t dtype;     /* SGB_F32 or SGB_F64                       */
+    int32_t dtype;     /* SGB_F32, SGB_F64, SGB_C64 or SGB_C128    */
     int32_t _pad;
     int64_t n;         /* number of diagonal blocks, >= 1          */
     int64_t b;         /* diagonal block size, >= 1                */
@@ -145,18 +154,23 @@ int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char tran
  * only (SGB_ERR_UNSUPPORTED otherwise); n >= 2.
  *
  * sgb_pobtaf_permuted: pobtaf(..., buffer=) (src/serinv/algs/pobtaf.py:
- *   58-76, _pobtaf_permuted :186-281).  Workspace: sgb_pobtaf_workspace_size.
- *   buffer[1] <- lower[0]^T first; buffer[0] is not touched.
+ *   58-76, _pobtaf_permuted :186-281).  Workspace:
+ *   sgb_pobtaf_permuted_workspace_size.  buffer[1] <- lower[0]^H first;
+ *   buffer[0] is not touched.
  * sgb_pobtasi_permuted: pobtasi(..., buffer=) (src/serinv/algs/pobtasi.py:
  *   54-71, _pobtasi_permuted :175-244).  On entry blocks 0 and n-1, arrow[0],
  *   arrow[n-1], tip and buffer[n-1] hold the reduced system's inverse.
  *   Workspace: sgb_pobtasi_permuted_workspace_size.
  * sgb_pobtas_permuted: pobtas(..., buffer=) (src/serinv/algs/pobtas.py:
- *   31-46, _pobtas_permuted :164-218).  Workspace: sgb_pobtas_workspace_size.
+ *   31-46, _pobtas_permuted :164-218).  Workspace:
+ *   sgb_pobtas_permuted_workspace_size.
+ * For real dtypes the permuted workspace sizes equal the natural ones.
  */
 int sgb_pobtaf_permuted(const sgb_bta* m, void* buffer, int precision, void* workspace,
                         size_t workspace_bytes, int32_t* info, void* stream);
+int sgb_pobtaf_permuted_workspace_size(const sgb_bta* m, int precision, size_t* bytes);
 int sgb_pobtasi_permuted_workspace_size(const sgb_bta* m, int precision, size_t* bytes);
+int sgb_pobtas_permuted_workspace_size(const sgb_bta* m, int64_t nrhs, int precision, size_t* bytes);
 int sgb_pobtasi_permuted(const sgb_bta* m, void* buffer, int precision, void* workspace,
                          size_t workspace_bytes, void* stream);
 int sgb_pobtas_permuted(const sgb_bta* m, void* buffer, void* rhs, int64_t nrhs, int64_t ldb,
@@ -235,7 +249,8 @@ int sgb_batch_plan_destroy(sgb_batch_plan* plan);
 #define SGB_KCLASS_GEMM_TC     3  /* tensor-core (tcgen05) block products      */
 #define SGB_KCLASS_SPLIT       4  /* operand slicing for the tensor-core path  */
 #define SGB_KCLASS_PANEL       5  /* persistent column-block Cholesky          */
-#define SGB_KCLASS_COUNT       6
+#define SGB_KCLASS_EMBED       6  /* complex <-> real embedding copies         */
+#define SGB_KCLASS_COUNT       7
 
 /* Number of kernels this library has launched since it was loaded. */
 long long sgb_launch_count(void);

@@ -26,6 +26,8 @@ SGB_ERR_UNSUPPORTED = 8
 
 SGB_F32 = 0
 SGB_F64 = 1
+SGB_C64 = 2
+SGB_C128 = 3
 
 SGB_PREC_NATIVE = 0
 SGB_PREC_MIXED = 1
@@ -79,8 +81,12 @@ _SIGNATURES = {
                                   ctypes.c_size_t, ctypes.c_void_p]),
     "sgb_pobtaf_permuted": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
+    "sgb_pobtaf_permuted_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int,
+                                                          ctypes.POINTER(ctypes.c_size_t)]),
     "sgb_pobtasi_permuted_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int,
                                                            ctypes.POINTER(ctypes.c_size_t)]),
+    "sgb_pobtas_permuted_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int64, ctypes.c_int,
+                                                          ctypes.POINTER(ctypes.c_size_t)]),
     "sgb_pobtasi_permuted": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_int,
                                             ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "sgb_pobtas_permuted": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_void_p,
@@ -113,7 +119,7 @@ _SIGNATURES = {
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 
-KCLASS = {"gemm": 0, "potrf_tile": 1, "trtri_tile": 2, "gemm_tc": 3, "split": 4, "panel": 5}
+KCLASS = {"gemm": 0, "potrf_tile": 1, "trtri_tile": 2, "gemm_tc": 3, "split": 4, "panel": 5, "embed": 6}
 
 _lock = threading.Lock()
 _lib = None

@@ -81,12 +81,15 @@ def _wrap(x, device: torch.device, name: str) -> _Arr:
         if x.is_cuda:
             if x.device != device:
                 raise ValueError(f"{name} is on {x.device}, expected {device}")
+            if x.is_conj() or x.is_neg():
+                # lazily conjugated / negated views: materialise, write back through the view
+                return _Arr(x.resolve_conj().resolve_neg().contiguous(), x, "devcopy")
             if x.is_contiguous():
                 return _Arr(x, x, "dev")
             return _Arr(x.contiguous(), x, "devcopy")
         # asynchronous from pinned memory, ordered before the library's
         # kernels on the same stream
-        return _Arr(x.to(device, non_blocking=True).contiguous(), x, "torch_host")
+        return _Arr(x.resolve_conj().resolve_neg().to(device, non_blocking=True).contiguous(), x, "torch_host")
     if isinstance(x, np.ndarray):
         if not x.flags.writeable:
             raise ValueError(f"{name} is read-only; the computation is in place")
@@ -108,8 +111,10 @@ def _dtype_code(dt: torch.dtype) -> int:
         return _lib.SGB_F64
     if dt == torch.float32:
         return _lib.SGB_F32
-    if dt in (torch.complex64, torch.complex128):
-        raise NotImplementedError("complex BTA matrices are not supported yet")
+    if dt == torch.complex128:
+        return _lib.SGB_C128
+    if dt == torch.complex64:
+        return _lib.SGB_C64
     raise TypeError(f"unsupported dtype {dt}")
 
 
@@ -338,7 +343,7 @@ def _pobtaf_permuted(D, Lo, Ar, T, buffer, kwargs):
     m = _bta_struct(*(x.t for x in w[:4]))
     with torch.cuda.device(device):
         nbytes = ctypes.c_size_t(0)
-        _lib.raise_for(lib.sgb_pobtaf_workspace_size(ctypes.byref(m), precision, ctypes.byref(nbytes)),
+        _lib.raise_for(lib.sgb_pobtaf_permuted_workspace_size(ctypes.byref(m), precision, ctypes.byref(nbytes)),
                        "pobtaf")
         ws = _workspace(nbytes.value, device)
         info = torch.zeros(1, dtype=torch.int32, device=device)
@@ -392,8 +397,8 @@ def _pobtas_permuted(D, Lo, Ar, T, B, buffer, trans, kwargs):
     nrhs = Bt.shape[1]
     with torch.cuda.device(device):
         nbytes = ctypes.c_size_t(0)
-        _lib.raise_for(lib.sgb_pobtas_workspace_size(ctypes.byref(m), nrhs, precision, ctypes.byref(nbytes)),
-                       "pobtas")
+        _lib.raise_for(lib.sgb_pobtas_permuted_workspace_size(ctypes.byref(m), nrhs, precision,
+                                                              ctypes.byref(nbytes)), "pobtas")
         ws = _workspace(nbytes.value, device)
         rc = lib.sgb_pobtas_permuted(ctypes.byref(m), _ptr(w[5].t), _ptr(Bt), nrhs, max(nrhs, 1), trans.encode(),
                                      precision, ws.data_ptr(), nbytes.value, _stream(device))

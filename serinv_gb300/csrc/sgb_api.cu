@@ -14,6 +14,12 @@ int cuda_fail(cudaError_t e) {
     return SGB_ERR_CUDA;
 }
 
+}  // namespace
+
+int record_cuda_error(cudaError_t e) { return cuda_fail(e); }
+
+namespace {
+
 #define SGB_TRY(expr)                                     \
     do {                                                  \
         cudaError_t _e = (expr);                          \
@@ -976,6 +982,7 @@ const char* sgb_strerror(int code) {
 int sgb_last_cuda_error(void) { return g_last_cuda_error; }
 
 int sgb_pobtaf_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
+    if (cx_dtype(m)) return cx_pobtaf_workspace_size(m, precision, bytes, false);
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -986,6 +993,7 @@ int sgb_pobtaf_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
 }
 
 int sgb_pobtasi_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
+    if (cx_dtype(m)) return cx_pobtasi_workspace_size(m, precision, bytes, false);
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -996,6 +1004,7 @@ int sgb_pobtasi_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
 }
 
 int sgb_pobtas_workspace_size(const sgb_bta* m, int64_t nrhs, int precision, size_t* bytes) {
+    if (cx_dtype(m)) return cx_pobtas_workspace_size(m, nrhs, precision, bytes, false);
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -1069,6 +1078,9 @@ int sgb_dgemm(int precision, char transA, char transB, int64_t M, int64_t N, int
 
 int sgb_pobtaf(const sgb_bta* m, int factorize_last_block, int precision, void* workspace,
                size_t workspace_bytes, int32_t* info, void* stream) {
+    if (cx_dtype(m))
+        return cx_pobtaf(m, factorize_last_block, precision, workspace, workspace_bytes, info,
+                         (cudaStream_t)stream, nullptr);
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -1085,6 +1097,9 @@ int sgb_pobtaf(const sgb_bta* m, int factorize_last_block, int precision, void* 
 
 int sgb_pobtasi(const sgb_bta* m, int invert_last_block, int precision, void* workspace, size_t workspace_bytes,
                 void* stream) {
+    if (cx_dtype(m))
+        return cx_pobtasi(m, invert_last_block, precision, workspace, workspace_bytes, (cudaStream_t)stream,
+                          nullptr);
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -1100,6 +1115,9 @@ int sgb_pobtasi(const sgb_bta* m, int invert_last_block, int precision, void* wo
 
 int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char trans, int partial, int precision,
                void* workspace, size_t workspace_bytes, void* stream) {
+    if (cx_dtype(m))
+        return cx_pobtas(m, rhs, nrhs, ldb, trans, partial, precision, workspace, workspace_bytes,
+                         (cudaStream_t)stream, nullptr);
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -1118,6 +1136,11 @@ int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char tran
 
 int sgb_pobtaf_permuted(const sgb_bta* m, void* buffer, int precision, void* workspace, size_t workspace_bytes,
                         int32_t* info, void* stream) {
+    if (cx_dtype(m)) {
+        if (buffer == nullptr) return SGB_ERR_ARG;
+        if (m->n < 2) return SGB_ERR_SHAPE;
+        return cx_pobtaf(m, 1, precision, workspace, workspace_bytes, info, (cudaStream_t)stream, buffer);
+    }
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -1126,7 +1149,7 @@ int sgb_pobtaf_permuted(const sgb_bta* m, void* buffer, int precision, void* wor
     if (m->n < 2) return SGB_ERR_SHAPE;
     if (buffer == nullptr) return SGB_ERR_ARG;
     size_t need = 0;
-    sgb_pobtaf_workspace_size(m, precision, &need);
+    sgb_pobtaf_permuted_workspace_size(m, precision, &need);
     if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
@@ -1134,7 +1157,18 @@ int sgb_pobtaf_permuted(const sgb_bta* m, void* buffer, int precision, void* wor
     return pobtaf_permuted_run<float>(m, (float*)buffer, workspace, info, s);
 }
 
+int sgb_pobtaf_permuted_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
+    if (cx_dtype(m)) return cx_pobtaf_workspace_size(m, precision, bytes, true);
+    return sgb_pobtaf_workspace_size(m, precision, bytes);
+}
+
+int sgb_pobtas_permuted_workspace_size(const sgb_bta* m, int64_t nrhs, int precision, size_t* bytes) {
+    if (cx_dtype(m)) return cx_pobtas_workspace_size(m, nrhs, precision, bytes, true);
+    return sgb_pobtas_workspace_size(m, nrhs, precision, bytes);
+}
+
 int sgb_pobtasi_permuted_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
+    if (cx_dtype(m)) return cx_pobtasi_workspace_size(m, precision, bytes, true);
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -1147,6 +1181,11 @@ int sgb_pobtasi_permuted_workspace_size(const sgb_bta* m, int precision, size_t*
 
 int sgb_pobtasi_permuted(const sgb_bta* m, void* buffer, int precision, void* workspace, size_t workspace_bytes,
                          void* stream) {
+    if (cx_dtype(m)) {
+        if (buffer == nullptr) return SGB_ERR_ARG;
+        if (m->n < 2) return SGB_ERR_SHAPE;
+        return cx_pobtasi(m, 1, precision, workspace, workspace_bytes, (cudaStream_t)stream, buffer);
+    }
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -1164,6 +1203,11 @@ int sgb_pobtasi_permuted(const sgb_bta* m, void* buffer, int precision, void* wo
 
 int sgb_pobtas_permuted(const sgb_bta* m, void* buffer, void* rhs, int64_t nrhs, int64_t ldb, char trans,
                         int precision, void* workspace, size_t workspace_bytes, void* stream) {
+    if (cx_dtype(m)) {
+        if (buffer == nullptr) return SGB_ERR_ARG;
+        return cx_pobtas(m, rhs, nrhs, ldb, trans, 0, precision, workspace, workspace_bytes,
+                         (cudaStream_t)stream, buffer);
+    }
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
@@ -1173,7 +1217,7 @@ int sgb_pobtas_permuted(const sgb_bta* m, void* buffer, void* rhs, int64_t nrhs,
     if (nrhs < 0 || nrhs > (1 << 20) || ldb < nrhs) return SGB_ERR_SHAPE;
     if ((nrhs > 0 && rhs == nullptr) || buffer == nullptr) return SGB_ERR_ARG;
     size_t need = 0;
-    sgb_pobtas_workspace_size(m, nrhs, precision, &need);
+    sgb_pobtas_permuted_workspace_size(m, nrhs, precision, &need);
     if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if (m->dtype == SGB_F64)

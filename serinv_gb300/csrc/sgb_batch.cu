@@ -78,6 +78,7 @@ int validate(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int cou
         it.precision = precisions ? precisions[i] : SGB_PREC_NATIVE;
         if ((ops & SGB_OP_POBTAS) && it.nrhs > 0 && it.rhs == nullptr) return SGB_ERR_ARG;
         if (it.nrhs < 0) return SGB_ERR_SHAPE;
+        if (it.m.dtype != SGB_F32 && it.m.dtype != SGB_F64) return SGB_ERR_DTYPE;  // real matrices only
         size_t x = 0;
         int rc = sgb_pobtaf_workspace_size(&it.m, it.precision, &x);
         if (rc) return rc;

@@ -155,6 +155,21 @@ cudaError_t tc_prepare();
 cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_bytes, int32_t* err,
                     cudaStream_t s);
 
+// Records e as this thread's last CUDA error; returns SGB_ERR_CUDA.
+int record_cuda_error(cudaError_t e);
+
+// Complex dtypes through the real embedding (sgb_complex.cu).  buffer !=
+// nullptr selects the permuted form.
+bool cx_dtype(const sgb_bta* m);
+int cx_pobtaf_workspace_size(const sgb_bta* m, int precision, size_t* bytes, bool permuted);
+int cx_pobtasi_workspace_size(const sgb_bta* m, int precision, size_t* bytes, bool permuted);
+int cx_pobtas_workspace_size(const sgb_bta* m, int64_t nrhs, int precision, size_t* bytes, bool permuted);
+int cx_pobtaf(const sgb_bta* m, int flb, int precision, void* ws, size_t ws_bytes, int32_t* info, cudaStream_t s,
+              void* buffer);
+int cx_pobtasi(const sgb_bta* m, int ilb, int precision, void* ws, size_t ws_bytes, cudaStream_t s, void* buffer);
+int cx_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char trans, int partial, int precision,
+              void* ws, size_t ws_bytes, cudaStream_t s, void* buffer);
+
 // Launch accounting (sgb_prof.cu): call prof_before just before and
 // prof_after just after every kernel launch.
 void prof_before(cudaStream_t s, int kclass = -1);

@@ -64,7 +64,10 @@ def generate(n: int, b: int, a: int, nrhs: int = 1, seed: int = 0,
 
     ``shift="dd"`` applies the diagonal-dominance shift; a float applies
     ``D_i += shift * I`` and ``T += shift * I`` instead (no dominance shift).
-    Values are drawn in float64 and rounded once to ``dtype``.
+    Values are drawn in float64 and rounded once to ``dtype``.  Complex
+    dtypes give a Hermitian positive-definite matrix: the imaginary parts
+    are drawn after the real ones (same order, same distribution), the
+    diagonal blocks and tip are ``R + R^H``, and the shift uses the moduli.
     """
     if n < 1 or b < 1 or a < 0 or nrhs < 0:
         raise ValueError("need n >= 1, b >= 1, a >= 0, nrhs >= 0")
@@ -74,10 +77,17 @@ def generate(n: int, b: int, a: int, nrhs: int = 1, seed: int = 0,
     Ar = _u(rng, (n, a, b))
     S = _u(rng, (a, a))
     B = _u(rng, (n * b + a, nrhs))
+    if np.issubdtype(np.dtype(dtype), np.complexfloating):
+        # imaginary parts drawn after the real ones, in the same order
+        R = R + 1j * _u(rng, R.shape)
+        Lo = Lo + 1j * _u(rng, Lo.shape)
+        Ar = Ar + 1j * _u(rng, Ar.shape)
+        S = S + 1j * _u(rng, S.shape)
+        B = B + 1j * _u(rng, B.shape)
 
-    D = R + R.transpose(0, 2, 1)
+    D = R + R.conj().transpose(0, 2, 1)   # Hermitian: real diagonal
     del R
-    T = S + S.T
+    T = S + S.conj().T
 
     if isinstance(shift, str):
         if shift != "dd":

@@ -45,8 +45,9 @@ def bench_digest():
 
 
 def rel_err(x, ref) -> float:
-    x = np.asarray(x, dtype=np.float64)
-    ref = np.asarray(ref, dtype=np.float64)
+    dt = np.complex128 if (np.iscomplexobj(x) or np.iscomplexobj(ref)) else np.float64
+    x = np.asarray(x, dtype=dt)
+    ref = np.asarray(ref, dtype=dt)
     den = np.linalg.norm(ref)
     if den == 0:
         return float(np.linalg.norm(x))

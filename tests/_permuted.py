@@ -16,7 +16,7 @@ def reduced(D, Ar, T, buf, zeros):
     rAr = zeros((2, a, b), D)
     rT = zeros((a, a), D)
     rD[0], rD[1] = D[0], D[-1]
-    rLo[0] = buf[-1].T
+    rLo[0] = buf[-1].conj().T
     rAr[0], rAr[1] = Ar[0], Ar[-1]
     rT[:, :] = T
     return rD, rLo, rAr, rT
@@ -24,7 +24,7 @@ def reduced(D, Ar, T, buf, zeros):
 
 def map_back(D, Ar, T, buf, rD, rLo, rAr, rT):
     D[0], D[-1] = rD[0], rD[1]
-    buf[-1] = rLo[0].T
+    buf[-1] = rLo[0].conj().T
     Ar[0], Ar[-1] = rAr[0], rAr[1]
     T[:, :] = rT
 

@@ -17,8 +17,8 @@ and the permuted middle-partition workflow (``buffer=``, as the
 reference's permuted tests drive it) on small synthetic inputs, and stores
 inputs and outputs (full arrays for small cases, a digest plus edge blocks
 for the 128x64 case) as compressed ``.npz`` files beside this script, with
-the NumPy/SciPy versions in ``versions.json``.  ``--only=permuted`` writes
-the permuted file alone.
+the NumPy/SciPy versions in ``versions.json``.  ``--only=permuted`` and
+``--only=complex`` write the permuted or the complex128 file alone.
 """
 
 from __future__ import annotations
@@ -111,8 +111,10 @@ def permuted_cases(ref, generate):
     permuted pobtasi / permuted pobtas N and C, on seeded synthetic inputs."""
     out = {}
     cases = []
-    for (n, b, a, nrhs, seed) in [(3, 5, 3, 2, 11), (4, 16, 4, 3, 12), (6, 40, 7, 2, 13), (5, 33, 1, 1, 14)]:
-        m = generate(n, b, a, nrhs, seed=seed)
+    for (n, b, a, nrhs, seed, dt) in [(3, 5, 3, 2, 11, np.float64), (4, 16, 4, 3, 12, np.float64),
+                                      (6, 40, 7, 2, 13, np.float64), (5, 33, 1, 1, 14, np.float64),
+                                      (5, 12, 3, 2, 15, np.complex128)]:
+        m = generate(n, b, a, nrhs, seed=seed, dtype=dt)
         D, Lo, Ar, T, B = (x.copy() for x in (m.D, m.Lo, m.Ar, m.T, m.B))
         buf = np.zeros_like(D)
         ref["pobtaf"](D, Lo, Ar, T, buffer=buf)
@@ -136,7 +138,7 @@ def permuted_cases(ref, generate):
         ref["pobtas"](*rL, rB, trans="C")
         x[:b], x[(n - 1) * b:n * b], x[n * b:] = rB[:b], rB[b:2 * b], rB[2 * b:]
         ref["pobtas"](LD, LLo, LAr, LT, x, buffer=Lbuf, trans="C")
-        key = f"n{n}_b{b}_a{a}_r{nrhs}_s{seed}_"
+        key = f"n{n}_b{b}_a{a}_r{nrhs}_s{seed}_" + ("c128_" if dt == np.complex128 else "")
         for name, arr in zip(("D", "Lo", "Ar", "T", "B"), (m.D, m.Lo, m.Ar, m.T, m.B)):
             out[f"{key}in_{name}"] = arr
         for name, arr in zip(("D", "Lo", "Ar", "T", "buf"), F):
@@ -149,11 +151,46 @@ def permuted_cases(ref, generate):
     np.savez_compressed(os.path.join(HERE, "permuted.npz"), **out)
 
 
+def complex_cases(ref, tu, generate):
+    """complex128: the reference suite's grid with its complex inputs
+    (``dd_bta(..., dtype="complex128")`` + ``symmetrize`` and ``rhs``, as its
+    tests run them) and seeded synthetic Hermitian shapes with non-zero
+    imaginary parts."""
+    out = {}
+    cases = []
+    for b in (2, 3):
+        for a in (2, 3):
+            for n in (1, 2, 3, 4):
+                nrhs = 2
+                # the dtype as its tests pass it (the string): the matrix is
+                # complex with real entries, the right-hand side complex
+                A = tu.dd_bta(b, a, n, device_array=False, dtype="complex128")
+                tu.symmetrize(A)
+                B = tu.rhs(nrhs, b, a, n, device_array=False, dtype="complex128")
+                (D, Lo, _, Ar, _, T) = tu.bta_dense_to_arrays(A, b, a, n)
+                L, X, x = _run_reference(ref, D, Lo, Ar, T, B)
+                key = f"suite_b{b}_a{a}_n{n}_r{nrhs}_"
+                out.update(_pack(key, D, Lo, Ar, T, B, L, X, x))
+                cases.append(key)
+    for (n, b, a, nrhs, seed) in [(3, 24, 7, 3, 21), (4, 33, 5, 1, 22), (5, 32, 0, 2, 23), (2, 16, 4, 2, 24),
+                                  (6, 40, 3, 2, 25)]:
+        m = generate(n, b, a, nrhs, seed=seed, dtype=np.complex128)
+        L, X, x = _run_reference(ref, m.D, m.Lo, m.Ar, m.T, m.B)
+        key = f"n{n}_b{b}_a{a}_r{nrhs}_s{seed}_"
+        out.update(_pack(key, m.D, m.Lo, m.Ar, m.T, m.B, L, X, x))
+        cases.append(key)
+    out["cases"] = np.array(cases)
+    np.savez_compressed(os.path.join(HERE, "complex.npz"), **out)
+
+
 def main(ref_root: str, only: str | None = None) -> None:
     ref, tu = _load_reference(ref_root)
     from serinv_gb300.synthetic import generate
     if only == "permuted":
         permuted_cases(ref, generate)
+        return
+    if only == "complex":
+        complex_cases(ref, tu, generate)
         return
 
     # 1) The reference test suite's own input family and parameter grid.
@@ -212,6 +249,10 @@ def main(ref_root: str, only: str | None = None) -> None:
 
     # 4) The permuted (middle-partition) variants.
     permuted_cases(ref, generate)
+
+    # 5) complex128 (a fresh load of the test utilities restarts their seed).
+    ref, tu = _load_reference(ref_root)
+    complex_cases(ref, tu, generate)
 
     import scipy
     with open(os.path.join(HERE, "versions.json"), "w") as f:

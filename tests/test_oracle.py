@@ -6,7 +6,7 @@ import pytest
 import oracle
 from serinv_gb300.synthetic import generate, flops
 
-from _golden import all_full_cases, bench_digest, rel_err
+from _golden import all_full_cases, bench_digest, load_cases, rel_err
 
 CASES = all_full_cases()
 
@@ -161,3 +161,33 @@ def test_permuted_workflow_is_the_inverse(case):
     for got, ref in ((X["D"], D), (X["Lo"], Lo), (X["Ar"], Ar), (X["T"], T)):
         assert rel_err(got, ref) <= 1e-10
     assert rel_err(x, np.linalg.solve(A, inp["B"])) <= 1e-10
+
+
+COMPLEX = load_cases("complex.npz")
+
+
+def _oracle_run(D, Lo, Ar, T, B):
+    oracle.pobtaf(D, Lo, Ar, T)
+    L = [x.copy() for x in (D, Lo, Ar, T)]
+    oracle.pobtasi(D, Lo, Ar, T)
+    oracle.pobtas(*L, B, trans="N")
+    oracle.pobtas(*L, B, trans="C")
+    return L, [D, Lo, Ar, T], B
+
+
+@pytest.mark.parametrize("case", COMPLEX, ids=[c[0] for c in COMPLEX])
+def test_oracle_complex_matches_reference(case):
+    """complex128: the restatement (conjugate transposes throughout) against
+    the reference's own outputs, and the outputs against dense NumPy."""
+    key, inp, L, X, x = case
+    D, Lo, Ar, T, B = (inp[k].copy() for k in ("D", "Lo", "Ar", "T", "B"))
+    Lg, Xg, xg = _oracle_run(D, Lo, Ar, T, B)
+    for got, ref in zip(Lg, L):
+        if ref.size:
+            assert rel_err(got, ref) <= 1e-12
+    for got, ref in zip(Xg, X):
+        if ref.size:
+            assert rel_err(got, ref) <= 1e-12
+    assert rel_err(xg, x) <= 1e-12
+    A = oracle.bta_to_dense(inp["D"], inp["Lo"], inp["Ar"], inp["T"])
+    assert rel_err(xg, np.linalg.solve(A, inp["B"])) <= 1e-10

@@ -18,7 +18,8 @@ from _permuted import workflow
 
 pytestmark = pytest.mark.gpu
 
-TOL = {np.dtype(np.float64): 1e-12, np.dtype(np.float32): 1e-5}
+TOL = {np.dtype(np.float64): 1e-12, np.dtype(np.float32): 1e-5, np.dtype(np.complex128): 1e-12,
+       np.dtype(np.complex64): 1e-5}
 PERM = permuted_cases()
 
 
