@@ -68,7 +68,10 @@ def parse():
     p.add_argument("--bare", action="store_true",
                    help="only the warm-up and timed steps (for profiler launch lists): no comparison form, "
                         "no accuracy run, no live FP64 peak, no e2e, no CPU baseline")
-    p.add_argument("--workload", choices=["bta", "batched", "kappa", "autograd"], default="bta")
+    p.add_argument("--workload", choices=["bta", "batched", "kappa", "autograd", "complex"], default="bta")
+    p.add_argument("--cx-n", type=int, default=256)
+    p.add_argument("--cx-b", type=int, default=256)
+    p.add_argument("--cx-a", type=int, default=32)
     p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--batch-precision", choices=["native", "mixed"], default="native")
     p.add_argument("--ag-n", type=int, default=1024)
@@ -579,6 +582,62 @@ def bench_autograd(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_complex(args):
+    """complex128 Hermitian pobtaf + pobtasi (default n=256, b=256, a=32)
+    through the real embedding, mixed and FP64 forms.  The metric counts the
+    canonical complex flops (4x the real count); the real sweeps run on the
+    embedded (n, 2b, 2a) matrix, twice those flops.  Device-resident inputs,
+    CUDA events around each pobtaf+pobtasi on torch's current stream (the
+    library's stream), a fresh copy of the inputs before each timed step
+    (outside the events; the stacks exceed L2 after embedding)."""
+    import torch
+
+    from serinv_gb300 import _lib, pobtaf, pobtasi
+    from serinv_gb300.synthetic import flops, generate_torch
+
+    torch.cuda.set_device(0)
+    _lib.load()
+    n, b, a = args.cx_n, args.cx_b, args.cx_a
+    src = generate_torch(n, b, a, 0, seed=0, dtype=torch.complex128)[:4]
+    fl = flops(n, b, a)
+    cflops = 4.0 * (fl["pobtaf"] + fl["pobtasi"])
+    fr = flops(n, 2 * b, 2 * a)
+    out = {}
+    for prec in ("mixed", "fp64"):
+        work = [x.clone() for x in src]
+        times = []
+        for it in range(args.warmup + args.steps):
+            for w, x in zip(work, src):
+                w.copy_(x)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            pobtaf(*work, precision=prec)
+            pobtasi(*work, precision=prec)
+            e1.record()
+            torch.cuda.synchronize()
+            if it >= args.warmup:
+                times.append(e0.elapsed_time(e1))
+        ms = float(np.median(times))
+        out[prec] = {"ms": ms, "value": cflops / (ms * 1e-3) / 1e12,
+                     "embedded_real_tflops": (fr["pobtaf"] + fr["pobtasi"]) / (ms * 1e-3) / 1e12,
+                     "X": [x.clone() for x in work]}
+    errs = {}
+    for name, g, r in zip(("diag", "lower", "arrow", "tip"), out["mixed"]["X"], out["fp64"]["X"]):
+        errs[name] = float(torch.linalg.vector_norm(g - r) / torch.linalg.vector_norm(r))
+    line = {"metric": "complex128 pobtaf+pobtasi throughput (canonical complex flops)",
+            "value": out["mixed"]["value"], "unit": "TFLOP/s", "higher_is_better": True,
+            "ms_per_step": out["mixed"]["ms"], "steps": args.steps, "warmup": args.warmup,
+            "dtype": "c128 (real embedding, FP64 storage; tensor-core slice products)",
+            "config": {"workload": f"complex128 Hermitian BTA n={n} b={b} a={a}", "n": n, "b": b, "a": a,
+                       "flops_complex": cflops, "flops_embedded_real": fr["pobtaf"] + fr["pobtasi"]},
+            "embedded_real_tflops": out["mixed"]["embedded_real_tflops"],
+            "compare": {"fp64": {"value": out["fp64"]["value"], "ms_per_step": out["fp64"]["ms"],
+                                 "embedded_real_tflops": out["fp64"]["embedded_real_tflops"]}},
+            "rel_err_mixed_vs_fp64": errs}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -587,7 +646,8 @@ def main():
         bench_reference(args, rank, world)
         return
     if args.workload != "bta":
-        {"batched": bench_batched, "kappa": bench_kappa, "autograd": bench_autograd}[args.workload](args)
+        {"batched": bench_batched, "kappa": bench_kappa, "autograd": bench_autograd,
+         "complex": bench_complex}[args.workload](args)
         return
     dist = None
     if world > 1:

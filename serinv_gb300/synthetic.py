@@ -147,7 +147,8 @@ def generate_torch(n: int, b: int, a: int, nrhs: int = 1, seed: int = 0, dtype=N
     Same draw order, distributions and dominance shift; different random
     numbers (torch's Philox stream, not NumPy's PCG64).  Used where the
     inputs are too large to draw on the host in reasonable time; parity
-    tests use ``generate``.  Returns (D, Lo, Ar, T, B) torch tensors.
+    tests use ``generate``.  Complex dtypes as in ``generate``.  Returns
+    (D, Lo, Ar, T, B) torch tensors.
     """
     import torch
 
@@ -162,9 +163,16 @@ def generate_torch(n: int, b: int, a: int, nrhs: int = 1, seed: int = 0, dtype=N
     Ar = u(n, a, b)
     S = u(a, a)
     B = u(n * b + a, nrhs)
-    D = R + R.transpose(1, 2)
+    if dtype.is_complex:
+        # imaginary parts drawn after the real ones, in the same order
+        R = torch.complex(R, u(n, b, b))
+        Lo = torch.complex(Lo, u(n - 1, b, b))
+        Ar = torch.complex(Ar, u(n, a, b))
+        S = torch.complex(S, u(a, a))
+        B = torch.complex(B, u(n * b + a, nrhs))
+    D = R + R.transpose(1, 2).conj()   # Hermitian: real diagonal
     del R
-    T = S + S.T
+    T = S + S.T.conj()
     idx = torch.arange(b, device=device)
     if isinstance(shift, str):
         rows = D.abs().sum(dim=2) - torch.diagonal(D, dim1=1, dim2=2).abs()
