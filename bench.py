@@ -505,6 +505,28 @@ def bench_kappa(args):
         res = {"kappa_target": kappa, "kappa_achieved": achieved, "sigma": sigma}
         ref = [x.clone() for x in (D, Lo, Ar, T)]
         sg.pobtaf(*ref)
+        # the solve: FP64 factor, and the mixed factor unrefined / refined
+        # against A (16 right-hand sides, torch generator seed 1)
+        g = torch.Generator(device="cuda").manual_seed(1)
+        B = torch.rand((N, 16), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+        A = (D, Lo, Ar, T)
+
+        def solve(L, iters):
+            x = B.clone()
+            sg.pobtas_refine(*A, *L, x, iters=iters)
+            r = sg.bta_matvec(*A, x, alpha=-1.0, beta=1.0, y=B.clone())
+            return x, float(torch.linalg.norm(r) / torch.linalg.norm(B))
+
+        x64, res64 = solve(ref, 0)
+        Lm = [x.clone() for x in A]
+        sg.pobtaf(*Lm, precision=args.precision, check_spd=False)
+        sol = {"fp64": {"rel_residual": res64}}
+        for iters in (0, 1, 2):
+            xm, rm = solve(Lm, iters)
+            sol[f"{args.precision}_refine{iters}"] = {
+                "rel_residual": rm, "rel_diff_vs_fp64": float(torch.linalg.norm(xm - x64) / torch.linalg.norm(x64))}
+        res["solve"] = sol
+        del Lm
         sg.pobtasi(*ref)
         for prec in [p for p in args.compare.split(",") if p] + [args.precision]:
             if prec == "fp64":
@@ -523,7 +545,7 @@ def bench_kappa(args):
                                      for nm, x, y in zip(("diag", "lower", "arrow", "tip"), X, ref)}}
         out.append(res)
         del ref
-    line = {"metric": "mixed-precision error vs conditioning (pobtaf+pobtasi against FP64)",
+    line = {"metric": "mixed-precision error vs conditioning (pobtaf+pobtasi against FP64; solve refined against A)",
             "config": {"n": n, "b": b, "a": a, "lanczos_A0": [lmin0, lmax0]}, "results": out}
     print(json.dumps(line), flush=True)
 

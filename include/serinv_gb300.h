@@ -178,6 +178,28 @@ int sgb_pobtas_permuted(const sgb_bta* m, void* buffer, void* rhs, int64_t nrhs,
                         void* stream);
 
 /*
+ * y <- alpha * A x + beta * y for the symmetric BTA matrix of A's lower
+ * stacks (only the lower triangles of diag and tip are read).  x and y are
+ * (n*b + a, nrhs) with leading dimensions ldx, ldy >= nrhs and must not
+ * overlap (SGB_ERR_ARG).  Real dtypes.  No workspace.
+ */
+int sgb_bta_symv(const sgb_bta* A, const void* x, int64_t ldx, void* y, int64_t ldy, int64_t nrhs,
+                 double alpha, double beta, void* stream);
+
+/*
+ * Refined solve: rhs <- A^{-1} rhs with the factor L of A (sgb_pobtaf, any
+ * precision) and `iters` steps of iterative refinement against the
+ * original A: x = L^{-T} L^{-1} b, then r = b - A x (sgb_bta_symv), x += L^{-T}
+ * L^{-1} r.  iters = 0 is the plain solve of sgb_pobtas (N then T).  A and L
+ * have the same shape and real dtype.  The reference's pobtas
+ * (src/serinv/algs/pobtas.py:10-62) has no refinement; this call serves the
+ * mixed-precision factor.
+ */
+int sgb_pobtas_refine_workspace_size(const sgb_bta* L, int64_t nrhs, size_t* bytes);
+int sgb_pobtas_refine(const sgb_bta* A, const sgb_bta* L, void* rhs, int64_t nrhs, int64_t ldb,
+                      int iters, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * sgb_pobtaf without a workspace argument, for callers that cannot allocate
  * device memory: code running while a stream is being captured, real-time
  * loops that forbid allocator calls, and foreign-language hosts that hold

@@ -10,5 +10,7 @@ __version__ = "0.1.0"
 
 from .algs import pobtaf, pobtasi, pobtas, pobtf, pobtsi, pobts  # noqa: E402,F401
 from .dense import dgemm  # noqa: E402,F401
+from .refine import bta_matvec, pobtas_refine  # noqa: E402,F401
 
-__all__ = ["pobtaf", "pobtasi", "pobtas", "pobtf", "pobtsi", "pobts", "dgemm", "__version__"]
+__all__ = ["pobtaf", "pobtasi", "pobtas", "pobtf", "pobtsi", "pobts", "dgemm", "bta_matvec", "pobtas_refine",
+           "__version__"]

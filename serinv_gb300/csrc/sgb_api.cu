@@ -580,7 +580,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
 // block step is two grouped products.
 template <typename T>
 int pobtas_native(const sgb_bta* m, T* Bm, int64_t nrhs, int64_t ldb, char trans, int partial, void* ws,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool have_linv = false) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
@@ -598,8 +598,11 @@ int pobtas_native(const sgb_bta* m, T* Bm, int64_t nrhs, int64_t ldb, char trans
 
     if (nrhs == 0) return SGB_OK;
     Ctx native;
-    SGB_TRY(trtri_run<T>(native, D, b, n, Linv, trs, s));
-    if (a && !partial) SGB_TRY(trtri_run<T>(native, Tp, a, 1, Ltinv, trs, s));
+    // have_linv: the workspace holds the inverses from an earlier call with this factor
+    if (!have_linv) {
+        SGB_TRY(trtri_run<T>(native, D, b, n, Linv, trs, s));
+        if (a && !partial) SGB_TRY(trtri_run<T>(native, Tp, a, 1, Ltinv, trs, s));
+    }
 
     if (trans == 'N') {
         const int64_t last = partial ? n - 1 : n;
@@ -955,6 +958,50 @@ int pobtas_permuted_run(const sgb_bta* m, T* buf, T* Bm, int64_t nrhs, int64_t l
     return SGB_OK;
 }
 
+// ---- refined solve ---------------------------------------------------------
+// x = A^{-1} B by the factor L, refined against the original A:
+//   x <- L^{-T} L^{-1} B ; repeat: r = B - A x, x += L^{-T} L^{-1} r.
+// The residual is formed in the storage precision from A's lower stacks;
+// the block inverses of L are formed once and reused by every solve.
+template <typename T>
+struct RefineWs {
+    size_t solve, x, r, total;
+    RefineWs(const sgb_bta* L, int64_t nrhs) {
+        const size_t N = (size_t)(L->n * L->b + L->a);
+        Carve c;
+        solve = c.take(PobtasWs<T>(L, nrhs).total);
+        x = c.take(sizeof(T) * N * (size_t)nrhs);
+        r = c.take(sizeof(T) * N * (size_t)nrhs);
+        total = c.off;
+    }
+};
+
+template <typename T>
+int pobtas_refine_run(const sgb_bta* A, const sgb_bta* L, T* B, int64_t nrhs, int64_t ldb, int iters, void* ws,
+                      cudaStream_t s) {
+    if (nrhs == 0) return SGB_OK;
+    RefineWs<T> W(L, nrhs);
+    char* base = (char*)ws;
+    void* sw = base + W.solve;
+    T* x = (T*)(base + W.x);
+    T* r = (T*)(base + W.r);
+    const int64_t N = L->n * L->b + L->a;
+    const size_t row = sizeof(T) * (size_t)nrhs;
+    SGB_TRY(cudaMemcpy2DAsync(x, row, B, sizeof(T) * ldb, row, N, cudaMemcpyDeviceToDevice, s));
+    int rc = pobtas_native<T>(L, x, nrhs, nrhs, 'N', 0, sw, s, false);
+    if (rc == SGB_OK) rc = pobtas_native<T>(L, x, nrhs, nrhs, 'C', 0, sw, s, true);
+    for (int k = 0; k < iters && rc == SGB_OK; ++k) {
+        SGB_TRY(cudaMemcpy2DAsync(r, row, B, sizeof(T) * ldb, row, N, cudaMemcpyDeviceToDevice, s));
+        SGB_TRY(bta_symv<T>(A, x, nrhs, r, nrhs, nrhs, T(-1), T(1), s));
+        rc = pobtas_native<T>(L, r, nrhs, nrhs, 'N', 0, sw, s, true);
+        if (rc == SGB_OK) rc = pobtas_native<T>(L, r, nrhs, nrhs, 'C', 0, sw, s, true);
+        if (rc == SGB_OK) SGB_TRY(axpy2d<T>(x, nrhs, r, nrhs, N, nrhs, s));
+    }
+    if (rc != SGB_OK) return rc;
+    SGB_TRY(cudaMemcpy2DAsync(B, sizeof(T) * ldb, x, row, row, N, cudaMemcpyDeviceToDevice, s));
+    return SGB_OK;
+}
+
 }  // namespace
 }  // namespace sgb
 
@@ -1223,6 +1270,52 @@ int sgb_pobtas_permuted(const sgb_bta* m, void* buffer, void* rhs, int64_t nrhs,
     if (m->dtype == SGB_F64)
         return pobtas_permuted_run<double>(m, (double*)buffer, (double*)rhs, nrhs, ldb, trans, workspace, s);
     return pobtas_permuted_run<float>(m, (float*)buffer, (float*)rhs, nrhs, ldb, trans, workspace, s);
+}
+
+int sgb_bta_symv(const sgb_bta* A, const void* x, int64_t ldx, void* y, int64_t ldy, int64_t nrhs, double alpha,
+                 double beta, void* stream) {
+    int rc = check_bta(A);
+    if (rc) return rc;
+    if (nrhs < 0 || nrhs > (1 << 20) || ldx < nrhs || ldy < nrhs) return SGB_ERR_SHAPE;
+    if (nrhs == 0) return SGB_OK;
+    if (x == nullptr || y == nullptr) return SGB_ERR_ARG;
+    const int64_t N = A->n * A->b + A->a;
+    const size_t es = A->dtype == SGB_F64 ? 8 : 4;
+    const uintptr_t xl = (uintptr_t)x, xh = xl + es * (size_t)((N - 1) * ldx + nrhs);
+    const uintptr_t yl = (uintptr_t)y, yh = yl + es * (size_t)((N - 1) * ldy + nrhs);
+    if (xl < yh && yl < xh) return SGB_ERR_ARG;  // x and y overlap
+    cudaStream_t s = (cudaStream_t)stream;
+    if (A->dtype == SGB_F64)
+        SGB_TRY(bta_symv<double>(A, (const double*)x, ldx, (double*)y, ldy, nrhs, alpha, beta, s));
+    else
+        SGB_TRY(bta_symv<float>(A, (const float*)x, ldx, (float*)y, ldy, nrhs, (float)alpha, (float)beta, s));
+    return SGB_OK;
+}
+
+int sgb_pobtas_refine_workspace_size(const sgb_bta* L, int64_t nrhs, size_t* bytes) {
+    int rc = check_bta(L);
+    if (rc) return rc;
+    if (!bytes) return SGB_ERR_ARG;
+    if (nrhs < 0 || nrhs > (1 << 20)) return SGB_ERR_SHAPE;
+    *bytes = L->dtype == SGB_F64 ? RefineWs<double>(L, nrhs).total : RefineWs<float>(L, nrhs).total;
+    return SGB_OK;
+}
+
+int sgb_pobtas_refine(const sgb_bta* A, const sgb_bta* L, void* rhs, int64_t nrhs, int64_t ldb, int iters,
+                      void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = check_bta(A);
+    if (rc) return rc;
+    if ((rc = check_bta(L))) return rc;
+    if (A->dtype != L->dtype || A->n != L->n || A->b != L->b || A->a != L->a) return SGB_ERR_SHAPE;
+    if (nrhs < 0 || nrhs > (1 << 20) || ldb < nrhs) return SGB_ERR_SHAPE;
+    if (iters < 0 || iters > 100) return SGB_ERR_ARG;
+    if (nrhs > 0 && rhs == nullptr) return SGB_ERR_ARG;
+    size_t need = 0;
+    sgb_pobtas_refine_workspace_size(L, nrhs, &need);
+    if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (A->dtype == SGB_F64) return pobtas_refine_run<double>(A, L, (double*)rhs, nrhs, ldb, iters, workspace, s);
+    return pobtas_refine_run<float>(A, L, (float*)rhs, nrhs, ldb, iters, workspace, s);
 }
 
 }  // extern "C"

@@ -247,6 +247,154 @@ __global__ void __launch_bounds__(NT) k_gemm_skinny(const __grid_constant__ Gemm
     }
 }
 
+// FP32 products with a 64 x 64 output tile per CTA (4 x 4 per thread,
+// 16-byte shared-memory operand reads, the next K slab fetched into
+// registers during the current slab's FMAs).  The FP32 pipe retires 128
+// FFMA per SM per clock, 64 times the FP64 rate, so FP32 products are bound
+// by operand traffic, not arithmetic: the 32 x 32 tile's one shared-memory
+// read per FMA caps it far below the FFMA rate.  Same problem semantics as
+// k_gemm_simt, including `lower_only` at its 32 x 32 granularity (an
+// element is written unless its 32 x 32 tile lies strictly above the
+// diagonal), so either kernel may serve a launch.
+constexpr int WB = 64, WK = 16;
+
+__global__ void __launch_bounds__(NT) k_gemm_wide(const __grid_constant__ GemmLaunch<float> L) {
+    __shared__ __align__(16) float As[WK][WB + 4];
+    __shared__ __align__(16) float Bs[WK][WB + 4];
+
+    const int tile = blockIdx.x;
+    int pi = 0;
+#pragma unroll 1
+    for (int q = 1; q < L.np; ++q)
+        if (tile >= L.p[q].tile_begin) pi = q;
+    const GemmProb<float>& P = L.p[pi];
+    int local = tile - P.tile_begin;
+    const int per_inst = P.tiles_m * P.tiles_n;
+    const int inst = local / per_inst;
+    local -= inst * per_inst;
+    const int tm = local / P.tiles_n;
+    const int tn = local - tm * P.tiles_n;
+    const int m0 = tm * WB, n0 = tn * WB;
+    if (P.lower_only && n0 >= m0 + WB) return;
+
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+
+#pragma unroll 1
+    for (int ti = 0; ti < P.nterms; ++ti) {
+        const GemmTerm<float>& t = P.term[ti];
+        const float* A = t.A + (int64_t)inst * t.strideA;
+        const float* B = t.B + (int64_t)inst * t.strideB;
+        int klo = 0, khi = t.K;
+        switch (t.kmode) {
+            case KM_GE_N0: klo = n0; break;
+            case KM_LT_N1: khi = min(t.K, n0 + WB); break;
+            case KM_GE_M0: klo = m0; break;
+            case KM_LT_M1: khi = min(t.K, m0 + WB); break;
+            default: break;
+        }
+        // slab element e = tid + 256 q (q < 4): A as (m, k), B as (k, n),
+        // with the index order that makes the global reads coalesced
+        float ra[4], rb[4];
+        auto fetch = [&](int k0) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = tid + NT * q;
+                int m, k;
+                if (t.transA) { m = e % WB; k = e / WB; }
+                else          { k = e % WK; m = e / WK; }
+                const int gm = m0 + m, gk = k0 + k;
+                ra[q] = (gm < P.M && gk < khi)
+                            ? (t.transA ? A[(int64_t)gk * t.lda + gm] : A[(int64_t)gm * t.lda + gk])
+                            : 0.f;
+                int n;
+                if (t.transB) { k = e % WK; n = e / WK; }
+                else          { n = e % WB; k = e / WB; }
+                const int gn = n0 + n;
+                const int gk2 = k0 + k;
+                rb[q] = (gn < P.N && gk2 < khi)
+                            ? (t.transB ? B[(int64_t)gn * t.ldb + gk2] : B[(int64_t)gk2 * t.ldb + gn])
+                            : 0.f;
+            }
+        };
+        auto park = [&]() {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = tid + NT * q;
+                int m, k;
+                if (t.transA) { m = e % WB; k = e / WB; }
+                else          { k = e % WK; m = e / WK; }
+                As[k][m] = ra[q];
+                int n;
+                if (t.transB) { k = e % WK; n = e / WK; }
+                else          { n = e % WB; k = e / WB; }
+                Bs[k][n] = rb[q];
+            }
+        };
+        if (klo < khi) fetch(klo);
+#pragma unroll 1
+        for (int k0 = klo; k0 < khi; k0 += WK) {
+            __syncthreads();  // the previous slab's reads are done
+            park();
+            __syncthreads();
+            if (k0 + WK < khi) fetch(k0 + WK);
+#pragma unroll
+            for (int kk = 0; kk < WK; ++kk) {
+                const float4 a = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+                const float4 b = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+                const float av[4] = {a.x, a.y, a.z, a.w};
+                const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+            }
+        }
+        __syncthreads();
+    }
+
+    float* C = P.Cout + (int64_t)inst * P.strideC;
+    const float* Ci = P.Cin ? P.Cin + (int64_t)inst * P.strideCin : nullptr;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int gm = m0 + ty * 4 + i;
+        if (gm >= P.M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int gn = n0 + tx * 4 + j;
+            if (gn >= P.N) continue;
+            if (P.lower_only && (gn >> 5) > (gm >> 5)) continue;
+            float v = P.alpha * acc[i][j];
+            if (Ci != nullptr && P.beta != 0.f) {
+                const float c = P.transCin ? Ci[(int64_t)gn * P.ldcin + gm] : Ci[(int64_t)gm * P.ldcin + gn];
+                v = fmaf(P.beta, c, v);
+            }
+            C[(int64_t)gm * P.ldc + gn] = v;
+        }
+    }
+}
+
+inline void launch_wide(const GemmLaunch<float>& L, unsigned grid, cudaStream_t s) {
+    k_gemm_wide<<<grid, NT, 0, s>>>(L);
+}
+inline void launch_wide(const GemmLaunch<double>&, unsigned, cudaStream_t) {}  // never selected
+
+// The wide kernel serves an FP32 launch when one of its problems has a
+// 64 x 64 output tile's worth of rows and columns (smaller problems of the
+// same launch ride along in partly empty tiles).
+template <typename T>
+bool wide_ok(const GemmProb<T>* probs, int np) {
+    if (sizeof(T) != 4) return false;
+    for (int i = 0; i < np; ++i)
+        if (probs[i].batch > 0 && probs[i].M >= WB && probs[i].N >= WB) return true;
+    return false;
+}
+
 // Bytes an operand of `rows` x `cols` (leading dimension ld) spans over the
 // batch, as [lo, hi).
 template <typename T>
@@ -322,11 +470,13 @@ cudaError_t gemm_simt(GemmProb<T>* probs, int np, cudaStream_t s) {
     L.np = 0;
     int64_t total = 0;
     const bool skinny = skinny_ok<T>(probs, np);
+    const bool wide = !skinny && wide_ok<T>(probs, np);
+    const int tile_m = skinny ? SK_ROWS : (wide ? WB : BM);
     for (int i = 0; i < np; ++i) {
         GemmProb<T> p = probs[i];
         if (p.M <= 0 || p.N <= 0 || p.batch <= 0) continue;
-        p.tiles_m = (int32_t)ceil_div(p.M, skinny ? SK_ROWS : BM);
-        p.tiles_n = skinny ? 1 : (int32_t)ceil_div(p.N, BN);
+        p.tiles_m = (int32_t)ceil_div(p.M, tile_m);
+        p.tiles_n = skinny ? 1 : (int32_t)ceil_div(p.N, wide ? WB : BN);
         p.tile_begin = (int32_t)total;
         total += (int64_t)p.tiles_m * p.tiles_n * p.batch;
         L.p[L.np++] = p;
@@ -339,6 +489,7 @@ cudaError_t gemm_simt(GemmProb<T>* probs, int np, cudaStream_t s) {
     for (int i = 0; i < L.np; ++i) fl += useful_flops<T>(L.p[i]);
     prof_before(s, SGB_KCLASS_GEMM);
     if (skinny) k_gemm_skinny<T><<<(unsigned)total, NT, 0, s>>>(L);
+    else if (wide) launch_wide(L, (unsigned)total, s);
     else k_gemm_simt<T><<<(unsigned)total, NT, 0, s>>>(L);
     prof_after(SGB_KCLASS_GEMM, s, fl);
     return cudaGetLastError();

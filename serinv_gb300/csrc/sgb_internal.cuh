@@ -155,6 +155,15 @@ cudaError_t tc_prepare();
 cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_bytes, int32_t* err,
                     cudaStream_t s);
 
+// y <- alpha A x + beta y for the symmetric BTA matrix of A's lower stacks
+// (sgb_refine.cu); x and y (n*b + a rows) must not overlap.
+template <typename T>
+cudaError_t bta_symv(const sgb_bta* A, const T* x, int64_t ldx, T* y, int64_t ldy, int64_t nrhs, T alpha, T beta,
+                     cudaStream_t s);
+// x += y over rows x cols.
+template <typename T>
+cudaError_t axpy2d(T* x, int64_t ldx, const T* y, int64_t ldy, int64_t rows, int64_t cols, cudaStream_t s);
+
 // Records e as this thread's last CUDA error; returns SGB_ERR_CUDA.
 int record_cuda_error(cudaError_t e);
 

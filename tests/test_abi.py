@@ -114,6 +114,23 @@ def test_permuted_entry_points_host_checks(lib):
         _lib.SGB_ERR_SHAPE
 
 
+def test_symv_and_refine_host_checks(lib):
+    m = _desc(n=4, b=8, a=2)
+    # x and y overlapping are rejected; bad leading dimensions too
+    assert lib.sgb_bta_symv(ctypes.byref(m), 0x1000, 2, 0x1008, 2, 2, 1.0, 0.0, None) == _lib.SGB_ERR_ARG
+    assert lib.sgb_bta_symv(ctypes.byref(m), 0x1000, 1, 0x100000, 2, 2, 1.0, 0.0, None) == _lib.SGB_ERR_SHAPE
+    sz = ctypes.c_size_t(0)
+    assert lib.sgb_pobtas_refine_workspace_size(ctypes.byref(m), 3, ctypes.byref(sz)) == 0
+    assert sz.value >= 2 * (4 * 8 + 2) * 3 * 8
+    other = _desc(n=4, b=8, a=3)
+    assert lib.sgb_pobtas_refine(ctypes.byref(m), ctypes.byref(other), 0x1000, 1, 1, 2, 0x1000, 1 << 30,
+                                 None) == _lib.SGB_ERR_SHAPE
+    assert lib.sgb_pobtas_refine(ctypes.byref(m), ctypes.byref(m), 0x1000, 1, 1, -1, 0x1000, 1 << 30,
+                                 None) == _lib.SGB_ERR_ARG
+    assert lib.sgb_pobtas_refine(ctypes.byref(m), ctypes.byref(m), 0x1000, 1, 1, 2, None, 0,
+                                 None) == _lib.SGB_ERR_WORKSPACE
+
+
 def test_error_mapping():
     with pytest.raises(ValueError):
         _lib.raise_for(_lib.SGB_ERR_SHAPE, "x")

@@ -104,6 +104,7 @@ def test_golden_bench_shape_n128_b64_a16():
 SHAPES = [
     (1, 1, 0, 1), (1, 5, 3, 2), (2, 31, 1, 3), (2, 32, 32, 1), (3, 33, 5, 4), (5, 40, 0, 2),
     (4, 65, 17, 3), (3, 100, 33, 5), (2, 128, 64, 16), (3, 512, 64, 16), (7, 64, 1, 1),
+    (4, 200, 24, 4),
 ]
 
 
