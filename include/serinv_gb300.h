@@ -147,6 +147,23 @@ int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char tran
                void* stream);
 
 /*
+ * Host-resident stacks (the reference's device_streaming mode, pobtaf.py:
+ * 284-524, pobtasi.py:247-496): `host` describes the caller's host arrays
+ * (pinned memory for overlap; pageable works, without overlap), `dev` a
+ * device copy of the same shape and dtype that the sweep works in (its
+ * contents on entry are ignored).  Every block is uploaded on a copy stream
+ * in sweep order and downloaded as soon as it is final, overlapped with the
+ * factorization or back-sweep; on completion of `stream` the host arrays
+ * hold the result, exactly as sgb_pobtaf / sgb_pobtasi leave device arrays.
+ * Workspace: sgb_pobtaf_workspace_size / sgb_pobtasi_workspace_size of
+ * `dev`.  Real dtypes.
+ */
+int sgb_pobtaf_host(const sgb_bta* host, const sgb_bta* dev, int factorize_last_block, int precision,
+                    void* workspace, size_t workspace_bytes, int32_t* info, void* stream);
+int sgb_pobtasi_host(const sgb_bta* host, const sgb_bta* dev, int invert_last_block, int precision,
+                     void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * Permuted (middle-partition) forms: the `buffer=` keyword of the reference
  * functions.  buffer (n, b, b) carries the fill-in between block 0 and the
  * eliminated blocks 1..n-2; blocks 0, n-1 and the tip form the reduced

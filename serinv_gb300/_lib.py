@@ -79,6 +79,10 @@ _SIGNATURES = {
     "sgb_pobtas": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                   ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                   ctypes.c_size_t, ctypes.c_void_p]),
+    "sgb_pobtaf_host": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
+    "sgb_pobtasi_host": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "sgb_pobtaf_permuted": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
     "sgb_pobtaf_permuted_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int,

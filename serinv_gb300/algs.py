@@ -10,9 +10,11 @@ exception types as the reference's sequential functions:
 Arrays may be torch tensors (CUDA or CPU), NumPy arrays, or any CUDA array
 exporting ``__dlpack__`` (CuPy).  Device arrays are used in place on the
 current torch stream; host arrays are copied to the GPU, processed, and
-copied back in place (the whole matrix fits in HBM, so the reference's
-``device_streaming`` mode needs no separate code path and is accepted as a
-no-op).  All arithmetic runs in ``libserinv_gb300.so``; if it cannot be
+copied back in place.  Pinned host stacks (pobtaf, pobtasi) stream: the
+blocks travel up in sweep order and back as soon as they are final,
+overlapped with the computation -- the reference's ``device_streaming``
+mode, taken whenever the host memory allows it (the keyword itself is
+accepted).  All arithmetic runs in ``libserinv_gb300.so``; if it cannot be
 loaded or no GPU is present, the call raises — there is no CPU fallback.
 
 Extensions (keyword-only, absent from the reference): ``precision`` —
@@ -180,6 +182,52 @@ def _finish(wrapped) -> None:
         torch.cuda.current_stream(wrapped[0].t.device).synchronize()
 
 
+def _pinned_host_stacks(arrays):
+    """The stacks as C-contiguous pinned host tensors sharing the callers'
+    memory (real dtype), or None when any of them is not one."""
+    out = []
+    for x in arrays:
+        if isinstance(x, np.ndarray):
+            if not (x.flags.c_contiguous and x.flags.writeable):
+                return None
+            t = torch.from_numpy(x)
+        elif isinstance(x, torch.Tensor) and not x.is_cuda:
+            if not x.is_contiguous() or x.is_conj() or x.is_neg():
+                return None
+            t = x
+        else:
+            return None
+        if t.numel() and not t.is_pinned():
+            return None
+        out.append(t)
+    if len({t.dtype for t in out}) != 1 or out[0].dtype not in (torch.float64, torch.float32):
+        return None
+    return out
+
+
+def _host_call(entry, size_query, host, what, precision, flag, with_info):
+    """Pinned host stacks: a device copy of the same shape is the working
+    set, blocks travel up and back overlapped with the sweep (the C entry
+    `entry`), and the call returns once the host arrays hold the result."""
+    lib = _lib.load()
+    device = torch.device("cuda", torch.cuda.current_device())
+    dev = [torch.empty(t.shape, dtype=t.dtype, device=device) for t in host]
+    mh = _bta_struct(*host)
+    md = _bta_struct(*dev)
+    with torch.cuda.device(device):
+        nbytes = ctypes.c_size_t(0)
+        _lib.raise_for(size_query(ctypes.byref(md), precision, ctypes.byref(nbytes)), what)
+        ws = _workspace(nbytes.value, device)
+        args = [ctypes.byref(mh), ctypes.byref(md), int(flag), precision, ws.data_ptr(), nbytes.value]
+        info = torch.zeros(1, dtype=torch.int32, device=device) if with_info else None
+        if with_info:
+            args.append(info.data_ptr())
+        args.append(_stream(device))
+        _lib.raise_for(entry(*args), what)
+        torch.cuda.current_stream(device).synchronize()
+    return ws, info
+
+
 # --------------------------------------------------------------------------
 # public API
 
@@ -203,6 +251,20 @@ def pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_a
     factorize_last_block = bool(kwargs.get("factorize_last_block", True))
     precision = _precision(kwargs)
     check = bool(kwargs.get("check_spd", True))
+
+    arrays = (A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_arrow_tip_block)
+    _device_of(arrays)  # no GPU: fail loudly before touching the arrays
+    host = _pinned_host_stacks(arrays)
+    if host is not None:
+        lib = _lib.load()
+        ws, info = _host_call(lib.sgb_pobtaf_host, lib.sgb_pobtaf_workspace_size, host, "pobtaf", precision,
+                              factorize_last_block, True)
+        _check_status(ws, precision, "pobtaf", always=check)
+        if check:
+            k = int(info.item())
+            if k > 0:
+                raise np.linalg.LinAlgError(f"{k}-th leading minor of the array is not positive definite")
+        return
 
     lib = _lib.load()
     device, w = _prepare(
@@ -242,6 +304,16 @@ def pobtasi(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_
                                  L_arrow_tip_block, kwargs["buffer"], kwargs)
     invert_last_block = bool(kwargs.get("invert_last_block", True))
     precision = _precision(kwargs)
+
+    arrays = (L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_arrow_tip_block)
+    _device_of(arrays)
+    host = _pinned_host_stacks(arrays)
+    if host is not None:
+        lib = _lib.load()
+        ws, _ = _host_call(lib.sgb_pobtasi_host, lib.sgb_pobtasi_workspace_size, host, "pobtasi", precision,
+                           invert_last_block, False)
+        _check_status(ws, precision, "pobtasi")
+        return
 
     lib = _lib.load()
     device, w = _prepare(

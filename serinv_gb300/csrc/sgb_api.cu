@@ -2,6 +2,8 @@
 // block sweeps of pobtaf / pobtasi / pobtas that enqueue the kernels.
 #include <string.h>
 
+#include <vector>
+
 #include "sgb_internal.cuh"
 
 namespace sgb {
@@ -284,12 +286,131 @@ GemmProb<T> copy_prob(T* dst, int64_t ldd, const T* src, int64_t lds, int64_t M,
     return p;
 }
 
+// ---- host-resident stacks --------------------------------------------------
+// The stacks live in host memory (pinned for overlap) and are staged in a
+// device copy of the same shape.  Uploads of every block are enqueued up
+// front on a copy stream in the order the sweep consumes them, with an event
+// per group of kLinkGroup blocks; the sweep waits for a group's event only
+// when it reaches the group.  Finished blocks go back on a second copy
+// stream a group at a time, ordered after the launches that finalised them.
+// The transfers overlap the factorization / back-sweep, so a host-array call
+// costs little more than the device-resident one.
+constexpr int64_t kLinkGroup = 8;
+
+struct HostLink {
+    const sgb_bta* h = nullptr;  // host stacks
+    const sgb_bta* d = nullptr;  // device stacks (same shape)
+    bool ascending = true;       // sweep order: pobtaf ascending, pobtasi descending
+    size_t es = 8;
+    cudaStream_t up = nullptr, down = nullptr;
+    std::vector<cudaEvent_t> up_ev, events;
+    int64_t waited = -1;
+    std::vector<int64_t> pending;
+    bool tip_pending = false;
+
+    cudaError_t event(cudaEvent_t* e) {
+        cudaError_t r = cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+        if (r == cudaSuccess) events.push_back(*e);
+        return r;
+    }
+    cudaError_t copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
+        return bytes ? cudaMemcpyAsync(dst, src, bytes, kind, st) : cudaSuccess;
+    }
+    cudaError_t block(int64_t i, bool to_dev, cudaStream_t st) {
+        const int64_t n = h->n, b = h->b, a = h->a;
+        const cudaMemcpyKind k = to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+        auto mv = [&](void* hb, void* db, int64_t off, int64_t cnt) {
+            char* hp = (char*)hb + es * off;
+            char* dp = (char*)db + es * off;
+            return to_dev ? copy(dp, hp, es * cnt, k, st) : copy(hp, dp, es * cnt, k, st);
+        };
+        cudaError_t r = mv(h->diag, d->diag, i * b * b, b * b);
+        if (r == cudaSuccess && i < n - 1) r = mv(h->lower, d->lower, i * b * b, b * b);
+        if (r == cudaSuccess && a) r = mv(h->arrow, d->arrow, i * a * b, a * b);
+        return r;
+    }
+    cudaError_t tip(bool to_dev, cudaStream_t st) {
+        const int64_t a = h->a;
+        if (!a) return cudaSuccess;
+        return to_dev ? copy(d->tip, h->tip, es * a * a, cudaMemcpyHostToDevice, st)
+                      : copy(h->tip, d->tip, es * a * a, cudaMemcpyDeviceToHost, st);
+    }
+    int64_t pos(int64_t i) const { return ascending ? i : h->n - 1 - i; }
+
+    // Enqueue every upload (the tip first) after the work already on s.
+    cudaError_t start(cudaStream_t s) {
+        cudaError_t r = cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking);
+        if (r == cudaSuccess) r = cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking);
+        cudaEvent_t e0;
+        if (r == cudaSuccess) r = event(&e0);
+        if (r == cudaSuccess) r = cudaEventRecord(e0, s);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(up, e0, 0);
+        if (r == cudaSuccess) r = tip(true, up);
+        const int64_t n = h->n;
+        for (int64_t p = 0; p < n && r == cudaSuccess; ++p) {
+            r = block(ascending ? p : n - 1 - p, true, up);
+            if (r == cudaSuccess && ((p + 1) % kLinkGroup == 0 || p == n - 1)) {
+                cudaEvent_t e;
+                r = event(&e);
+                if (r == cudaSuccess) r = cudaEventRecord(e, up);
+                if (r == cudaSuccess) up_ev.push_back(e);
+            }
+        }
+        return r;
+    }
+    // Block i (and every block before it in sweep order, and the tip) resident.
+    cudaError_t need(int64_t i, cudaStream_t s) {
+        const int64_t g = pos(i) / kLinkGroup;
+        if (g <= waited) return cudaSuccess;
+        waited = g;
+        return cudaStreamWaitEvent(s, up_ev[(size_t)g], 0);
+    }
+    cudaError_t flush(cudaStream_t s) {
+        if (pending.empty() && !tip_pending) return cudaSuccess;
+        cudaEvent_t e;
+        cudaError_t r = event(&e);
+        if (r == cudaSuccess) r = cudaEventRecord(e, s);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(down, e, 0);
+        for (int64_t i : pending)
+            if (r == cudaSuccess) r = block(i, false, down);
+        if (r == cudaSuccess && tip_pending) r = tip(false, down);
+        pending.clear();
+        tip_pending = false;
+        return r;
+    }
+    // Block i is final once the launches enqueued so far on s have run.
+    cudaError_t give(int64_t i, cudaStream_t s) {
+        pending.push_back(i);
+        return (int64_t)pending.size() >= kLinkGroup ? flush(s) : cudaSuccess;
+    }
+    cudaError_t give_tip() {
+        tip_pending = true;
+        return cudaSuccess;
+    }
+    // The remaining downloads, then s waits for them.
+    cudaError_t finish(cudaStream_t s) {
+        cudaError_t r = flush(s);
+        cudaEvent_t e;
+        if (r == cudaSuccess) r = event(&e);
+        if (r == cudaSuccess) r = cudaEventRecord(e, down);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(s, e, 0);
+        return r;
+    }
+    ~HostLink() {
+        // released once their pending work completes
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+        if (up) cudaStreamDestroy(up);
+        if (down) cudaStreamDestroy(down);
+    }
+};
+
 // ---- pobtaf -------------------------------------------------------------
 // Block Cholesky, src/serinv/algs/pobtaf.py:97-183.  Per block i:
 //   [D_i; Lo_i; Ar_i] <- blocked Cholesky of the column block  (:117-139)
 //   D_{i+1} -= Lo_i Lo_i^T, Ar_{i+1} -= Ar_i Lo_i^T, T -= Ar_i Ar_i^T  (:143-159)
 template <typename T>
-int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int32_t* info, cudaStream_t s) {
+int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int32_t* info, cudaStream_t s,
+               HostLink* hl = nullptr) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
@@ -358,11 +479,15 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
         return e == cudaSuccess ? SGB_OK : cuda_fail(e);
     };
 
+    if (hl) SGB_TRY(hl->start(s));
     for (int64_t i = 0; i < n - 1; ++i) {
         RowSet<T> r1{Lo + i * bb, b, b};
         RowSet<T> r2{a ? Ar + i * ab : nullptr, a, b};
+        if (hl) SGB_TRY(hl->need(i, s));
         int rc = factor(i, r1, r2);
         if (rc != SGB_OK) return rc;
+        if (hl) SGB_TRY(hl->give(i, s));
+        if (hl) SGB_TRY(hl->need(i + 1, s));
 
         const bool next_factored = (i + 1 < n - 1) || factorize_last_block;
         GemmProb<T> pr[3];
@@ -401,6 +526,7 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
         SGB_TRY(run_gemm<T>(cx, pr, np, s));
     }
 
+    if (hl) SGB_TRY(hl->need(n - 1, s));
     if (factorize_last_block) {
         const int64_t i = n - 1;
         RowSet<T> r1{nullptr, 0, b};
@@ -421,6 +547,11 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
             rc = (int)factor_column_block<T>(Tp, a, a, none, none, tinv, info, n * b, s);  // :183
             if (rc != cudaSuccess) return cuda_fail((cudaError_t)rc);
         }
+    }
+    if (hl) {
+        SGB_TRY(hl->give(n - 1, s));
+        SGB_TRY(hl->give_tip());
+        SGB_TRY(hl->finish(s));
     }
     return SGB_OK;
 }
@@ -444,7 +575,8 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
 // Lo_i and Ar_i are dead once G_i, H_i, P_i exist, so P_i is formed in the
 // diagonal block itself and the outputs overwrite the factor in place.
 template <typename T>
-int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaStream_t s) {
+int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaStream_t s,
+                HostLink* hl = nullptr) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
@@ -463,6 +595,10 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
     T* GH = (T*)(base + W.gh);
     const int64_t bb = b * b, ab = a * b, ghs = (b + a) * b;
 
+    if (hl) {
+        SGB_TRY(hl->start(s));
+        SGB_TRY(hl->need(n - 1, s));
+    }
     if (invert_last_block && a) {
         // X_T = L_T^{-T} L_T^{-1}  (:115-119)
         SGB_TRY(trtri_run<T>(cx, Tp, a, 1, Ltinv, trs, s));
@@ -473,12 +609,14 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
         p.ldc = a;
         SGB_TRY(run_gemm<T>(cx, &p, 1, s));
     }
+    if (hl) SGB_TRY(hl->give_tip());
 
     // blocks whose L_ii is inverted here: all, or all but the last
     const int64_t ninv = invert_last_block ? n : n - 1;
     const int64_t tcb = S ? (W.chunk < kSiTcBatch ? W.chunk : kSiTcBatch) : W.chunk;
     for (int64_t hi = ninv; hi > 0; hi -= W.chunk) {
         const int64_t lo = hi > W.chunk ? hi - W.chunk : 0;
+        if (hl) SGB_TRY(hl->need(lo, s));
         SGB_TRY(trtri_run<T>(cx, D + lo * bb, b, hi - lo, Linv, trs, s));
         for (int64_t j0 = lo; j0 < hi; j0 += tcb) {
             const int64_t jn = (hi - j0) < tcb ? (hi - j0) : tcb;
@@ -554,22 +692,28 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
                 p.ldc = b;
                 pr[np++] = p;
             }
-            if (np == 0) continue;  // a == 0 and no next block: X_ii = P_i
-            SGB_TRY(run_gemm<T>(cx, pr, np, s));
-            // X_ii = P_i - X_{i+1,i}^T G_i - X_{A,i}^T H_i  (:164-169, :133-137)
-            GemmProb<T> p = prob<T>();
-            p.M = p.N = (int32_t)b;
-            int t = 0;
-            if (has_next) set_term<T>(p, t++, Lo + i * bb, b, 1, G, b, 0, b);
-            if (a) set_term<T>(p, t++, Ar + i * ab, b, 1, H, b, 0, a);
-            p.alpha = T(-1);
-            p.beta = T(1);
-            p.Cin = D + i * bb;
-            p.ldcin = b;
-            p.Cout = D + i * bb;
-            p.ldc = b;
-            SGB_TRY(run_gemm<T>(cx, &p, 1, s));
+            if (np > 0) {  // (a == 0 and no next block: X_ii = P_i)
+                SGB_TRY(run_gemm<T>(cx, pr, np, s));
+                // X_ii = P_i - X_{i+1,i}^T G_i - X_{A,i}^T H_i  (:164-169, :133-137)
+                GemmProb<T> p = prob<T>();
+                p.M = p.N = (int32_t)b;
+                int t = 0;
+                if (has_next) set_term<T>(p, t++, Lo + i * bb, b, 1, G, b, 0, b);
+                if (a) set_term<T>(p, t++, Ar + i * ab, b, 1, H, b, 0, a);
+                p.alpha = T(-1);
+                p.beta = T(1);
+                p.Cin = D + i * bb;
+                p.ldcin = b;
+                p.Cout = D + i * bb;
+                p.ldc = b;
+                SGB_TRY(run_gemm<T>(cx, &p, 1, s));
+            }
+            if (hl) SGB_TRY(hl->give(i, s));
         }
+    }
+    if (hl) {
+        if (!invert_last_block) SGB_TRY(hl->give(n - 1, s));
+        SGB_TRY(hl->finish(s));
     }
     return SGB_OK;
 }
@@ -1316,6 +1460,58 @@ int sgb_pobtas_refine(const sgb_bta* A, const sgb_bta* L, void* rhs, int64_t nrh
     cudaStream_t s = (cudaStream_t)stream;
     if (A->dtype == SGB_F64) return pobtas_refine_run<double>(A, L, (double*)rhs, nrhs, ldb, iters, workspace, s);
     return pobtas_refine_run<float>(A, L, (float*)rhs, nrhs, ldb, iters, workspace, s);
+}
+
+// Host-resident stacks: `host` holds the caller's (pinned) host arrays, `dev`
+// a device copy of the same shape that the sweep works in.
+int check_host_pair(const sgb_bta* host, const sgb_bta* dev) {
+    int rc = check_bta(host);
+    if (rc) return rc;
+    if ((rc = check_bta(dev))) return rc;
+    if (host->dtype != dev->dtype || host->n != dev->n || host->b != dev->b || host->a != dev->a)
+        return SGB_ERR_SHAPE;
+    return SGB_OK;
+}
+
+int sgb_pobtaf_host(const sgb_bta* host, const sgb_bta* dev, int factorize_last_block, int precision,
+                    void* workspace, size_t workspace_bytes, int32_t* info, void* stream) {
+    int rc = check_host_pair(host, dev);
+    if (rc) return rc;
+    const int S = parse_precision(precision, dev->dtype);
+    if (S < 0) return -S;
+    size_t need = 0;
+    sgb_pobtaf_workspace_size(dev, precision, &need);
+    if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
+    SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
+    HostLink hl;
+    hl.h = host;
+    hl.d = dev;
+    hl.ascending = true;
+    hl.es = dev->dtype == SGB_F64 ? 8 : 4;
+    if (dev->dtype == SGB_F64) return pobtaf_run<double>(dev, factorize_last_block, S, workspace, info, s, &hl);
+    return pobtaf_run<float>(dev, factorize_last_block, S, workspace, info, s, &hl);
+}
+
+int sgb_pobtasi_host(const sgb_bta* host, const sgb_bta* dev, int invert_last_block, int precision,
+                     void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = check_host_pair(host, dev);
+    if (rc) return rc;
+    const int S = parse_precision(precision, dev->dtype);
+    if (S < 0) return -S;
+    size_t need = 0;
+    sgb_pobtasi_workspace_size(dev, precision, &need);
+    if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
+    HostLink hl;
+    hl.h = host;
+    hl.d = dev;
+    hl.ascending = false;
+    hl.es = dev->dtype == SGB_F64 ? 8 : 4;
+    if (dev->dtype == SGB_F64) return pobtasi_run<double>(dev, invert_last_block, S, workspace, s, &hl);
+    return pobtasi_run<float>(dev, invert_last_block, S, workspace, s, &hl);
 }
 
 }  // extern "C"
