@@ -395,6 +395,13 @@ def bench_ours(args, rank: int, world: int, dist):
             "clocks": clk,
             "hbm_bytes_algorithmic_per_step": 2 * nbytes_sweep(n, b, a),
         }
+        # whole-step canonical TFLOP/s against the FP64 and bf16 tensor peaks
+        pk = measured_peaks()
+        line["peak_fractions"] = {
+            "of_fp64_dgemm_live": value / roof["peak"] if roof and roof.get("bound") == "fp64-pipe" else None,
+            "of_bf16_tensor": value / pk["bf16_tflops"] if pk.get("bf16_tflops") else None,
+            "note": "canonical pobtaf+pobtasi flops per second over cuBLAS DGEMM measured live, and over the "
+                    "bf16 dense tensor peak of MEASURED_PEAKS.json (of measured)"}
         print(json.dumps(line), flush=True)
 
 
