@@ -410,7 +410,7 @@ struct HostLink {
 //   D_{i+1} -= Lo_i Lo_i^T, Ar_{i+1} -= Ar_i Lo_i^T, T -= Ar_i Ar_i^T  (:143-159)
 template <typename T>
 int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int32_t* info, cudaStream_t s,
-               HostLink* hl = nullptr) {
+               HostLink* hl = nullptr, T* xall = nullptr, bool* xall_filled = nullptr) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
@@ -424,7 +424,7 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
     cx.tc_bytes = L.tc_bytes;
     cx.status = (int32_t*)((char*)ws + L.status);
     const int64_t bb = b * b, ab = a * b;
-    T* Xinv = (T*)((char*)ws + L.xinv);
+    T* Xinv0 = (T*)((char*)ws + L.xinv);
 
     // [D_i; rows below] <- Cholesky of the column block.  Native: one
     // blocked sweep over the tall column block (the TRSMs fold into the
@@ -436,19 +436,21 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
     SGB_TRY(cudaStreamIsCapturing(s, &cap));
     // one cooperative launch per block (on part of the GPU when captured
     // into a graph beside other work, if the capturing thread allows it);
-    // small blocks, and captures that do not, use the launch-based sweep
-    // (FP64 only there: an FP32 column block's FP32 arithmetic is cheap, and
-    // its launch-based sweep holds far fewer SMs than the persistent grid)
+    // small blocks, and captures that do not, use the launch-based sweep.
+    // In a batch graph the one launch per block also beats the ~25 launches
+    // of an FP32 block's tile sweep (measured on the uneven batch: 4.5 %)
     const bool captured = cap != cudaStreamCaptureStatusNone;
-    const int pgrid = captured && sizeof(T) == 8 ? capture_panel_grid() : 0;
+    const int pgrid = captured ? capture_panel_grid() : 0;
     const bool persistent = (!captured || pgrid > 0) && b > 2 * kTile;
     // 7 slices is the accuracy mode: its TRSMs stay FP64 substitutions (the
     // product with L_ii^{-T} carries kappa(L_ii) times the slice truncation)
     bool mixed_inverse = S != 0 && S < 7 && persistent;
     // the launch writes only the upper block triangle of L_ii^{-T}
-    if (mixed_inverse) SGB_TRY(cudaMemsetAsync(Xinv, 0, sizeof(T) * bb, s));
+    // xall (n b x b blocks): keep every L_ii^{-T} for later sweeps on this factor
+    if (mixed_inverse) SGB_TRY(cudaMemsetAsync(xall ? xall : Xinv0, 0, sizeof(T) * bb * (xall ? n : 1), s));
     auto factor = [&](int64_t i, RowSet<T> r1, RowSet<T> r2) -> int {
         T* Di = D + i * bb;
+        T* Xinv = xall ? xall + i * bb : Xinv0;
         if (mixed_inverse) {
             RowSet<T> none{nullptr, 0, b};
             cudaError_t e =
@@ -553,6 +555,7 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
         SGB_TRY(hl->give_tip());
         SGB_TRY(hl->finish(s));
     }
+    if (xall_filled) *xall_filled = xall != nullptr && mixed_inverse && factorize_last_block;
     return SGB_OK;
 }
 
@@ -576,7 +579,7 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
 // diagonal block itself and the outputs overwrite the factor in place.
 template <typename T>
 int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaStream_t s,
-                HostLink* hl = nullptr) {
+                HostLink* hl = nullptr, const T* xall = nullptr) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
@@ -617,11 +620,13 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
     for (int64_t hi = ninv; hi > 0; hi -= W.chunk) {
         const int64_t lo = hi > W.chunk ? hi - W.chunk : 0;
         if (hl) SGB_TRY(hl->need(lo, s));
-        SGB_TRY(trtri_run<T>(cx, D + lo * bb, b, hi - lo, Linv, trs, s));
+        // with xall the inverses exist already, as L_jj^{-T}: operands are read transposed
+        if (!xall) SGB_TRY(trtri_run<T>(cx, D + lo * bb, b, hi - lo, Linv, trs, s));
         for (int64_t j0 = lo; j0 < hi; j0 += tcb) {
             const int64_t jn = (hi - j0) < tcb ? (hi - j0) : tcb;
             const int64_t ng = (j0 + jn <= n - 1) ? jn : (n - 1 - j0);  // blocks with a Lo_j
-            T* Lj = Linv + (j0 - lo) * bb;
+            const T* Lj = xall ? xall + j0 * bb : Linv + (j0 - lo) * bb;
+            const int tl = xall ? 1 : 0;  // L_jj^{-1} = op(Lj)
             T* GHj = GH + (j0 - lo) * ghs;
             GemmProb<T> pr[3];
             int np = 0;
@@ -629,7 +634,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
                 GemmProb<T> p = prob<T>();
                 p.M = p.N = (int32_t)b;
                 p.batch = (int32_t)ng;
-                set_term<T>(p, 0, Lo + j0 * bb, b, 0, Lj, b, 0, b, KM_GE_N0);
+                set_term<T>(p, 0, Lo + j0 * bb, b, 0, Lj, b, tl, b, KM_GE_N0);
                 p.term[0].strideA = bb;
                 p.term[0].strideB = bb;
                 p.Cout = GHj;
@@ -642,7 +647,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
                 p.M = (int32_t)a;
                 p.N = (int32_t)b;
                 p.batch = (int32_t)jn;
-                set_term<T>(p, 0, Ar + j0 * ab, b, 0, Lj, b, 0, b, KM_GE_N0);
+                set_term<T>(p, 0, Ar + j0 * ab, b, 0, Lj, b, tl, b, KM_GE_N0);
                 p.term[0].strideA = ab;
                 p.term[0].strideB = bb;
                 p.Cout = GHj + bb;
@@ -654,7 +659,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
                 GemmProb<T> p = prob<T>();
                 p.M = p.N = (int32_t)b;
                 p.batch = (int32_t)jn;
-                set_term<T>(p, 0, Lj, b, 1, Lj, b, 0, b, KM_GE_M0);
+                set_term<T>(p, 0, Lj, b, 1 - tl, Lj, b, tl, b, KM_GE_M0);
                 p.term[0].strideA = bb;
                 p.term[0].strideB = bb;
                 p.Cout = D + j0 * bb;
@@ -724,7 +729,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
 // block step is two grouped products.
 template <typename T>
 int pobtas_native(const sgb_bta* m, T* Bm, int64_t nrhs, int64_t ldb, char trans, int partial, void* ws,
-                  cudaStream_t s, bool have_linv = false) {
+                  cudaStream_t s, bool have_linv = false, const T* xall = nullptr) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
@@ -744,9 +749,12 @@ int pobtas_native(const sgb_bta* m, T* Bm, int64_t nrhs, int64_t ldb, char trans
     Ctx native;
     // have_linv: the workspace holds the inverses from an earlier call with this factor
     if (!have_linv) {
-        SGB_TRY(trtri_run<T>(native, D, b, n, Linv, trs, s));
+        // with xall the block inverses exist already, as L_ii^{-T} (read transposed)
+        if (!xall) SGB_TRY(trtri_run<T>(native, D, b, n, Linv, trs, s));
         if (a && !partial) SGB_TRY(trtri_run<T>(native, Tp, a, 1, Ltinv, trs, s));
     }
+    const T* Li = xall ? xall : Linv;
+    const int tl = xall ? 1 : 0;
 
     if (trans == 'N') {
         const int64_t last = partial ? n - 1 : n;
@@ -755,7 +763,7 @@ int pobtas_native(const sgb_bta* m, T* Bm, int64_t nrhs, int64_t ldb, char trans
             GemmProb<T> p = prob<T>();
             p.M = (int32_t)b;
             p.N = (int32_t)nrhs;
-            set_term<T>(p, 0, Linv + i * bb, b, 0, Bi(i), ldb, 0, b, KM_LT_M1);
+            set_term<T>(p, 0, Li + i * bb, b, tl, Bi(i), ldb, 0, b, KM_LT_M1);
             p.Cout = y;
             p.ldc = nrhs;
             SGB_TRY(gemm_simt<T>(&p, 1, s));
@@ -837,7 +845,7 @@ int pobtas_native(const sgb_bta* m, T* Bm, int64_t nrhs, int64_t ldb, char trans
         GemmProb<T> q = prob<T>();
         q.M = (int32_t)b;
         q.N = (int32_t)nrhs;
-        set_term<T>(q, 0, Linv + i * bb, b, 1, Bi(i), ldb, 0, b, KM_GE_M0);
+        set_term<T>(q, 0, Li + i * bb, b, 1 - tl, Bi(i), ldb, 0, b, KM_GE_M0);
         q.Cout = y;
         q.ldc = nrhs;
         SGB_TRY(gemm_simt<T>(&q, 1, s));
@@ -1146,6 +1154,83 @@ int pobtas_refine_run(const sgb_bta* A, const sgb_bta* L, T* B, int64_t nrhs, in
     return SGB_OK;
 }
 
+// ---- batch plan items ------------------------------------------------------
+// pobtaf -> pobtas (N, T) -> pobtasi of one matrix inside a batch plan.  In
+// the mixed form with the persistent column-block kernel every L_ii^{-T} is
+// formed by pobtaf anyway; the item keeps them (n b x b blocks at the front
+// of its workspace) so that the solve and the selected inversion skip their
+// batched triangular inversions.
+bool item_keeps_inverses(const sgb_bta* m, int precision, int ops) {
+    const int S = parse_precision(precision, m->dtype);
+    return (ops & SGB_OP_POBTAF) && (ops & (SGB_OP_POBTAS | SGB_OP_POBTASI)) && m->dtype == SGB_F64 && S > 0 &&
+           S < 7 && m->b > 2 * kTile && capture_panel_grid() > 0;
+}
+
+}  // namespace
+
+size_t plan_item_ws(const sgb_bta* m, int ops, int precision, int64_t nrhs) {
+    size_t need = 0, x = 0;
+    if (ops & SGB_OP_POBTAF) {
+        sgb_pobtaf_workspace_size(m, precision, &x);
+        need = need > x ? need : x;
+    }
+    if (ops & SGB_OP_POBTASI) {
+        sgb_pobtasi_workspace_size(m, precision, &x);
+        need = need > x ? need : x;
+    }
+    if ((ops & SGB_OP_POBTAS) && nrhs > 0) {
+        sgb_pobtas_workspace_size(m, nrhs, precision, &x);
+        need = need > x ? need : x;
+    }
+    need = align_up(need);
+    if (item_keeps_inverses(m, precision, ops)) need += align_up(sizeof(double) * (size_t)(m->n * m->b * m->b));
+    return need;
+}
+
+int plan_item(const sgb_bta* m, int ops, int precision, void* rhs, int64_t nrhs, void* ws, size_t wsb,
+              int32_t* info, cudaStream_t s) {
+    if (!item_keeps_inverses(m, precision, ops)) {
+        int rc = SGB_OK;
+        if (ops & SGB_OP_POBTAF) rc = sgb_pobtaf(m, 1, precision, ws, wsb, info, s);
+        if (rc == SGB_OK && (ops & SGB_OP_POBTAS) && nrhs > 0) {
+            rc = sgb_pobtas(m, rhs, nrhs, nrhs, 'N', 0, precision, ws, wsb, s);
+            if (rc == SGB_OK) rc = sgb_pobtas(m, rhs, nrhs, nrhs, 'T', 0, precision, ws, wsb, s);
+        }
+        if (rc == SGB_OK && (ops & SGB_OP_POBTASI)) rc = sgb_pobtasi(m, 1, precision, ws, wsb, s);
+        return rc;
+    }
+    int rc = check_bta(m);
+    if (rc) return rc;
+    const int S = parse_precision(precision, m->dtype);
+    const size_t xbytes = align_up(sizeof(double) * (size_t)(m->n * m->b * m->b));
+    if (wsb < xbytes) return SGB_ERR_WORKSPACE;
+    double* xall = (double*)ws;
+    void* w = (char*)ws + xbytes;
+    const size_t wb = wsb - xbytes;
+    size_t need = 0;
+    sgb_pobtaf_workspace_size(m, precision, &need);
+    if ((rc = check_ws(w, wb, need))) return rc;
+    if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
+    SGB_TRY(cudaMemsetAsync(w, 0, sizeof(int32_t), s));  // status word
+    bool filled = false;
+    if ((rc = pobtaf_run<double>(m, 1, S, w, info, s, nullptr, xall, &filled))) return rc;
+    const double* xa = filled ? xall : nullptr;
+    if ((ops & SGB_OP_POBTAS) && nrhs > 0) {
+        sgb_pobtas_workspace_size(m, nrhs, precision, &need);
+        if ((rc = check_ws(w, wb, need))) return rc;
+        rc = pobtas_native<double>(m, (double*)rhs, nrhs, nrhs, 'N', 0, w, s, false, xa);
+        if (rc == SGB_OK) rc = pobtas_native<double>(m, (double*)rhs, nrhs, nrhs, 'T', 0, w, s, false, xa);
+        if (rc) return rc;
+    }
+    if (ops & SGB_OP_POBTASI) {
+        sgb_pobtasi_workspace_size(m, precision, &need);
+        if ((rc = check_ws(w, wb, need))) return rc;
+        rc = pobtasi_run<double>(m, 1, S, w, s, nullptr, xa);
+    }
+    return rc;
+}
+
+namespace {
 }  // namespace
 }  // namespace sgb
 

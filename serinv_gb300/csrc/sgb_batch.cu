@@ -39,19 +39,10 @@ struct Item {
 };
 
 size_t item_ws(const Item& it, int ops) {
-    size_t need = 0, x = 0;
-    if (ops & SGB_OP_POBTAF) {
-        sgb_pobtaf_workspace_size(&it.m, it.precision, &x);
-        need = std::max(need, x);
-    }
-    if (ops & SGB_OP_POBTASI) {
-        sgb_pobtasi_workspace_size(&it.m, it.precision, &x);
-        need = std::max(need, x);
-    }
-    if ((ops & SGB_OP_POBTAS) && it.nrhs > 0) {
-        sgb_pobtas_workspace_size(&it.m, it.nrhs, it.precision, &x);
-        need = std::max(need, x);
-    }
+    // sized as the plan's capture runs the item (its panel grid set)
+    sgb::set_capture_panel_grid(kPlanPanelGrid);
+    const size_t need = sgb::plan_item_ws(&it.m, ops, it.precision, it.nrhs);
+    sgb::set_capture_panel_grid(0);
     return (need + 255) / 256 * 256;
 }
 
@@ -189,12 +180,7 @@ int sgb_batch_plan_create(const sgb_bta* mats, void* const* rhs, const int64_t* 
         void* ws = (char*)workspace + L.stream_off[k];
         const size_t wsb = L.stream_bytes[k];
         void* s = (void*)streams[k];
-        if (ops & SGB_OP_POBTAF) rc = sgb_pobtaf(&it.m, 1, it.precision, ws, wsb, plan->info + i, s);
-        if (rc == SGB_OK && (ops & SGB_OP_POBTAS) && it.nrhs > 0) {
-            rc = sgb_pobtas(&it.m, it.rhs, it.nrhs, it.nrhs, 'N', 0, it.precision, ws, wsb, s);
-            if (rc == SGB_OK) rc = sgb_pobtas(&it.m, it.rhs, it.nrhs, it.nrhs, 'T', 0, it.precision, ws, wsb, s);
-        }
-        if (rc == SGB_OK && (ops & SGB_OP_POBTASI)) rc = sgb_pobtasi(&it.m, 1, it.precision, ws, wsb, s);
+        rc = sgb::plan_item(&it.m, ops, it.precision, it.rhs, it.nrhs, ws, wsb, plan->info + i, (cudaStream_t)s);
     }
     for (int k = 0; k < ns && e == cudaSuccess && rc == SGB_OK; ++k) {
         e = cudaEventRecord(events[k], streams[k]);

@@ -164,6 +164,11 @@ cudaError_t bta_symv(const sgb_bta* A, const T* x, int64_t ldx, T* y, int64_t ld
 template <typename T>
 cudaError_t axpy2d(T* x, int64_t ldx, const T* y, int64_t ldy, int64_t rows, int64_t cols, cudaStream_t s);
 
+// One matrix of a batch plan (sgb_api.cu): its workspace size and the ops.
+size_t plan_item_ws(const sgb_bta* m, int ops, int precision, int64_t nrhs);
+int plan_item(const sgb_bta* m, int ops, int precision, void* rhs, int64_t nrhs, void* ws, size_t wsb,
+              int32_t* info, cudaStream_t s);
+
 // Records e as this thread's last CUDA error; returns SGB_ERR_CUDA.
 int record_cuda_error(cudaError_t e);
 
