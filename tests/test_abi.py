@@ -131,6 +131,31 @@ def test_symv_and_refine_host_checks(lib):
                                  None) == _lib.SGB_ERR_WORKSPACE
 
 
+def test_complex_and_host_entry_points_host_checks(lib):
+    m = _desc(n=4, b=8, a=2)
+    c = _desc(n=4, b=8, a=2, dtype=_lib.SGB_C128)
+    real, cx = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(m), 0, ctypes.byref(real)) == 0
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(c), 0, ctypes.byref(cx)) == 0
+    # the embedded stacks (blocks 2b, arrow 2a) follow the real workspace
+    assert cx.value >= real.value + 8 * (4 * 16 * 16 + 3 * 16 * 16 + 4 * 4 * 16 + 4 * 4)
+    perm = ctypes.c_size_t(0)
+    assert lib.sgb_pobtaf_permuted_workspace_size(ctypes.byref(c), 0, ctypes.byref(perm)) == 0
+    assert perm.value > cx.value  # plus the embedded buffer
+    assert lib.sgb_pobtaf(ctypes.byref(c), 1, 0, None, 0, None, None) == _lib.SGB_ERR_WORKSPACE
+    c64 = _desc(n=4, b=8, a=2, dtype=_lib.SGB_C64)
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(c64), _lib.SGB_PREC_MIXED, ctypes.byref(cx)) == \
+        _lib.SGB_ERR_UNSUPPORTED
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(c), _lib.SGB_PREC_MIXED, ctypes.byref(cx)) == 0
+    # host-resident entries: shapes must match, workspace checked before any launch
+    other = _desc(n=4, b=8, a=3)
+    assert lib.sgb_pobtaf_host(ctypes.byref(m), ctypes.byref(other), 1, 0, 0x1000, 1 << 30, None, None) == \
+        _lib.SGB_ERR_SHAPE
+    assert lib.sgb_pobtaf_host(ctypes.byref(m), ctypes.byref(m), 1, 0, None, 0, None, None) == \
+        _lib.SGB_ERR_WORKSPACE
+    assert lib.sgb_pobtasi_host(ctypes.byref(m), ctypes.byref(m), 1, 0, None, 0, None) == _lib.SGB_ERR_WORKSPACE
+
+
 def test_error_mapping():
     with pytest.raises(ValueError):
         _lib.raise_for(_lib.SGB_ERR_SHAPE, "x")

@@ -79,3 +79,19 @@ def test_no_gpu_fails_loudly(m):
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         sg.pobtaf(*m.arrays())
     np.testing.assert_array_equal(m.D, before)
+
+
+def test_pinned_host_stack_detection_rejects_unsuitable_arrays(m):
+    """Only C-contiguous, writable, real, pinned host stacks take the streamed
+    path; everything else keeps the copy path."""
+    from serinv_gb300.algs import _pinned_host_stacks
+    arrs = list(m.arrays())
+    assert _pinned_host_stacks(arrs) is None  # pageable NumPy memory
+    ro = [x.copy() for x in arrs]
+    ro[0].flags.writeable = False
+    assert _pinned_host_stacks(ro) is None
+    nc = [x.copy() for x in arrs]
+    nc[0] = np.asfortranarray(nc[0])
+    assert _pinned_host_stacks(nc) is None
+    cx = [x.astype(np.complex128) for x in arrs]
+    assert _pinned_host_stacks(cx) is None
