@@ -2,7 +2,7 @@
 
 ``BatchPlan(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"),
 precisions=None, nstreams=None)`` takes a list of ``(D, Lo, Ar, T)`` torch
-CUDA stacks (float32 or float64, uneven n, b, a) and optional right-hand
+CUDA stacks (float32, float64, complex64 or complex128; uneven n, b, a) and optional right-hand
 sides ``(n*b+a, nrhs)``, and builds the C-level plan
 (``sgb_batch_plan_create``): the matrices are spread over ``nstreams``
 concurrent streams and their sweeps captured into one CUDA graph.
@@ -55,7 +55,8 @@ class BatchPlan:
         self.ops = sum(_OPS[o] for o in ops)
         if precisions is None:
             precisions = ["fp64"] * len(mats)
-        self.precisions = [_lib.precision_code(p) if m[0].dtype == torch.float64 else _lib.SGB_PREC_NATIVE
+        self.precisions = [_lib.precision_code(p) if m[0].dtype in (torch.float64, torch.complex128)
+                           else _lib.SGB_PREC_NATIVE
                            for p, m in zip(precisions, mats)]
         if nstreams is None:
             nstreams = autotune_nstreams(mats, rhs, ops, precisions)

@@ -49,9 +49,11 @@ size_t item_ws(const Item& it, int ops) {
 // Rough device time: FP64 work at ~0.6 TF/s, FP32 at ~8x that, plus a fixed
 // latency per 32-wide diagonal tile (the sequential pivot chain).
 double item_cost(const sgb_bta& m) {
-    const double n = (double)m.n, b = (double)m.b, a = (double)m.a;
+    // complex matrices run as their real embedding (blocks 2b, arrow 2a)
+    const bool cx = m.dtype == SGB_C64 || m.dtype == SGB_C128;
+    const double n = (double)m.n, b = (cx ? 2.0 : 1.0) * m.b, a = (cx ? 2.0 : 1.0) * m.a;
     const double fl = n * (26.0 / 3.0 * b * b * b + 10.0 * a * b * b + 3.0 * a * a * b);
-    const double rate = m.dtype == SGB_F64 ? 0.6e12 : 4.8e12;
+    const double rate = (m.dtype == SGB_F64 || m.dtype == SGB_C128) ? 0.6e12 : 4.8e12;
     const double tiles = n * std::ceil(b / 32.0);
     return fl / rate + tiles * 30e-6;
 }
@@ -69,7 +71,6 @@ int validate(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int cou
         it.precision = precisions ? precisions[i] : SGB_PREC_NATIVE;
         if ((ops & SGB_OP_POBTAS) && it.nrhs > 0 && it.rhs == nullptr) return SGB_ERR_ARG;
         if (it.nrhs < 0) return SGB_ERR_SHAPE;
-        if (it.m.dtype != SGB_F32 && it.m.dtype != SGB_F64) return SGB_ERR_DTYPE;  // real matrices only
         size_t x = 0;
         int rc = sgb_pobtaf_workspace_size(&it.m, it.precision, &x);
         if (rc) return rc;

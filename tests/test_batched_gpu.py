@@ -128,3 +128,30 @@ def test_batch_column_block_kernel_in_graph(precision):
                 assert rel_err(got.cpu().numpy(), ref) <= tol
         assert rel_err(r.cpu().numpy(), x) <= tol
     plan.close()
+
+
+def test_batch_with_complex_matrices():
+    """complex128 / complex64 matrices (through the real embedding) beside
+    real ones in one plan."""
+    rng = np.random.default_rng(5)
+    mats = []
+    for i in range(6):
+        n = int(rng.integers(2, 6))
+        b = int(rng.choice([8, 40, 96]))
+        a = int(rng.choice([0, 4]))
+        dt = [np.complex128, np.complex64, np.float64][i % 3]
+        mats.append(generate(n, b, a, 2, seed=200 + i, dtype=dt))
+    dev = [tuple(torch.from_numpy(x).cuda() for x in m.arrays()) for m in mats]
+    rhs = [torch.from_numpy(m.B).cuda() for m in mats]
+    plan = BatchPlan(dev, rhs, nstreams=3)
+    plan.run()
+    torch.cuda.synchronize()
+    assert torch.all(plan.info() == 0)
+    tol = {np.dtype(np.complex128): 1e-12, np.dtype(np.complex64): 1e-5, np.dtype(np.float64): 1e-12}
+    for m, d, r in zip(mats, dev, rhs):
+        L, X, x = oracle_run(m)
+        for got, ref in zip(d, X):
+            if ref.size:
+                assert rel_err(got.cpu().numpy(), ref) <= tol[m.D.dtype]
+        assert rel_err(r.cpu().numpy(), x) <= tol[m.D.dtype]
+    plan.close()
