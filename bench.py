@@ -256,10 +256,24 @@ def _timed_sweeps(torch, sg, _lib, A, A0, prec, steps, warmup, local, dist):
     prof_step = _lib.profile_read()
     _lib.profile_enable(False)
     if dist is not None:
-        t = torch.tensor([elapsed], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+        elapsed = max_over_ranks(dist, elapsed, "cuda")
     return elapsed / steps, launches, (prof, prof_step), clk
+
+
+def max_over_ranks(dist, value: float, device) -> float:
+    """The largest of every rank's `value` (the job's time is its slowest
+    replica's); every rank gets the result."""
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(step_flops: float, world: int, per_step_s: float) -> float:
+    """Whole-job TFLOP/s of `world` independent replicas, each doing one
+    step of `step_flops` per `per_step_s` (the slowest replica's time)."""
+    return step_flops * world / per_step_s / 1e12
 
 
 def _roofline(torch, profs):
@@ -315,7 +329,7 @@ def bench_ours(args, rank: int, world: int, dist):
 
     per_step, launches, prof, clk = _timed_sweeps(torch, sg, _lib, A, A0, prec, args.steps, args.warmup,
                                                   local, dist)
-    value = step_flops * world / per_step / 1e12
+    value = replica_throughput(step_flops, world, per_step)
 
     # the comparison forms (e.g. the FP64 drop-in beside the mixed form)
     compare = {}
