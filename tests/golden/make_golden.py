@@ -108,7 +108,8 @@ def _map_back(D, Ar, T, buf, rD, rLo, rAr, rT):
 def permuted_cases(ref, generate):
     """The middle-partition workflow of the reference's permuted tests:
     permuted pobtaf -> reduced system (pobtaf, then pobtasi or pobtas) ->
-    permuted pobtasi / permuted pobtas N and C, on seeded synthetic inputs."""
+    permuted pobtasi / permuted pobtas N and C, on seeded synthetic inputs;
+    one case of the arrow-free family (pobtf / pobtsi / pobts)."""
     out = {}
     cases = []
     for (n, b, a, nrhs, seed, dt) in [(3, 5, 3, 2, 11, np.float64), (4, 16, 4, 3, 12, np.float64),
@@ -144,6 +145,41 @@ def permuted_cases(ref, generate):
         for name, arr in zip(("D", "Lo", "Ar", "T", "buf"), F):
             out[f"{key}F_{name}"] = arr
         for name, arr in zip(("D", "Lo", "Ar", "T", "buf"), (XD, XLo, XAr, XT, Xbuf)):
+            out[f"{key}X_{name}"] = arr
+        out[f"{key}x"] = x
+        cases.append(key)
+    # the arrow-free family (pobtf / pobtsi / pobts with buffer=), same workflow
+    for (n, b, nrhs, seed) in [(5, 24, 2, 16)]:
+        m = generate(n, b, 0, nrhs, seed=seed)
+        D, Lo, B = m.D.copy(), m.Lo.copy(), m.B.copy()
+        buf = np.zeros_like(D)
+        ref["pobtf"](D, Lo, buffer=buf)
+        F = [x.copy() for x in (D, Lo, buf)]
+        rD = np.stack([D[0], D[-1]])
+        rLo = buf[-1].conj().T[None].copy()
+        ref["pobtf"](rD, rLo)
+        rL = [rD.copy(), rLo.copy()]
+        XD, XLo, Xbuf = D.copy(), Lo.copy(), buf.copy()
+        sD, sLo = rD.copy(), rLo.copy()
+        ref["pobtsi"](sD, sLo)
+        XD[0], XD[-1], Xbuf[-1] = sD[0], sD[1], sLo[0].conj().T
+        ref["pobtsi"](XD, XLo, buffer=Xbuf)
+        LD, LLo, Lbuf = D.copy(), Lo.copy(), buf.copy()
+        LD[0], LD[-1], Lbuf[-1] = rL[0][0], rL[0][1], rL[1][0].conj().T
+        x = B.copy()
+        ref["pobts"](LD, LLo, x, buffer=Lbuf, trans="N")
+        rB = np.concatenate([x[:b], x[(n - 1) * b:n * b]])
+        ref["pobts"](*rL, rB, trans="N")
+        ref["pobts"](*rL, rB, trans="C")
+        x[:b], x[(n - 1) * b:n * b] = rB[:b], rB[b:]
+        ref["pobts"](LD, LLo, x, buffer=Lbuf, trans="C")
+        key = f"bt_n{n}_b{b}_a0_r{nrhs}_s{seed}_"
+        ear, et = np.zeros((n, 0, b)), np.zeros((0, 0))
+        for name, arr in zip(("D", "Lo", "Ar", "T", "B"), (m.D, m.Lo, ear, et, m.B)):
+            out[f"{key}in_{name}"] = arr
+        for name, arr in zip(("D", "Lo", "Ar", "T", "buf"), (F[0], F[1], ear, et, F[2])):
+            out[f"{key}F_{name}"] = arr
+        for name, arr in zip(("D", "Lo", "Ar", "T", "buf"), (XD, XLo, ear, et, Xbuf)):
             out[f"{key}X_{name}"] = arr
         out[f"{key}x"] = x
         cases.append(key)
