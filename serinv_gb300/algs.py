@@ -6,6 +6,12 @@ exception types as the reference's sequential functions:
 * ``pobtaf``  — src/serinv/algs/pobtaf.py:11-94
 * ``pobtasi`` — src/serinv/algs/pobtasi.py:10-89
 * ``pobtas``  — src/serinv/algs/pobtas.py:10-62
+* ``pobtf`` / ``pobtsi`` / ``pobts`` — src/serinv/algs/pobtf.py, pobtsi.py,
+  pobts.py (the same calls with an empty arrow stack)
+
+``buffer=`` selects the permuted middle-partition forms (storage precision).
+float64, float32, complex128 and complex64 stacks are accepted; complex
+matrices are Hermitian and run through their real embedding.
 
 Arrays may be torch tensors (CUDA or CPU), NumPy arrays, or any CUDA array
 exporting ``__dlpack__`` (CuPy).  Device arrays are used in place on the
