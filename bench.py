@@ -180,7 +180,7 @@ def run_oracle_sample(n_s: int, b: int, a: int):
 def bench_reference(args, rank: int, world: int):
     if rank != 0:
         return
-    n_s = max(2, min(args.cpu_sample_blocks // 2, args.n))
+    n_s = max(2, min(args.cpu_sample_blocks, args.n))
     for _ in range(args.warmup):
         run_oracle_sample(max(2, n_s // 4), args.b, args.a)
     vals, times = [], []
@@ -260,6 +260,26 @@ def _timed_sweeps(torch, sg, _lib, A, A0, prec, steps, warmup, local, dist):
     return elapsed / steps, launches, (prof, prof_step), clk
 
 
+def _per_call_ms(torch, sg, A, A0, prec):
+    """One extra step with CUDA events around each call: device ms of
+    pobtaf and of pobtasi (median of three)."""
+    s = torch.cuda.current_stream()
+    out = {"pobtaf": [], "pobtasi": []}
+    for _ in range(3):
+        for x, y in zip(A, A0):
+            x.copy_(y)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(s)
+        sg.pobtaf(*A, precision=prec, check_spd=False)
+        ev[1].record(s)
+        sg.pobtasi(*A, precision=prec)
+        ev[2].record(s)
+        ev[2].synchronize()
+        out["pobtaf"].append(ev[0].elapsed_time(ev[1]))
+        out["pobtasi"].append(ev[1].elapsed_time(ev[2]))
+    return {k: float(np.median(v)) for k, v in out.items()}
+
+
 def max_over_ranks(dist, value: float, device) -> float:
     """The largest of every rank's `value` (the job's time is its slowest
     replica's); every rank gets the result."""
@@ -276,7 +296,17 @@ def replica_throughput(step_flops: float, world: int, per_step_s: float) -> floa
     return step_flops * world / per_step_s / 1e12
 
 
-def _roofline(torch, profs):
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
+# capture of the same kernel at the same block sizes (the per-launch traffic
+# of one block step does not depend on n): key (kernel class, precision, b, a).
+# Source: profiles/launches_mixed_fp64_bench_n64_b512_a64.md (column-block
+# kernel DRAM traffic, launches 70-72).
+TRAFFIC_PER_LAUNCH = {
+    ("panel", "mixed", 512, 64): 1.24e6 + 0.6e3,
+}
+
+
+def _roofline(torch, profs, prec="mixed", b=512, a=64):
     """Dominant kernel class of the profiled step; its achieved rate from the
     timed region's events when that class was timed there."""
     prof_timed, prof_step = profs
@@ -295,11 +325,29 @@ def _roofline(torch, profs):
         peak, src = peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (of measured)"
     else:
         peak, src = fp64_peak_live(torch), "cuBLAS DGEMM 4096^3 measured live (of measured)"
-    return {"bound": "tensor" if k == "gemm_tc" else "fp64-pipe", "kernel": k,
-            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "peak_source": src, "traffic": None,
-            "avg_launch_ms": d["ms"] / d["launches"], "events_from": where,
-            "share_of_device_time": share}
+    form = "mixed" if prec.startswith("mixed") else "fp64"
+    traffic = TRAFFIC_PER_LAUNCH.get((k, form, b, a))
+    out = {"bound": "tensor" if k == "gemm_tc" else "fp64-pipe", "kernel": k,
+           "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+           "peak_source": src, "traffic": traffic,
+           "traffic_note": ("DRAM bytes per launch, ncu capture of the same kernel at these block sizes "
+                            "(profiles/launches_mixed_fp64_bench_n64_b512_a64.md)") if traffic else None,
+           "algorithmic_bytes_per_launch": (8.0 * 3 * b * b) if k == "panel" and form == "mixed" else None,
+           "avg_launch_ms": d["ms"] / d["launches"], "events_from": where,
+           "share_of_device_time": share}
+    # the tensor-core products: bf16 flops the MMA warps issue over their
+    # event time in the profiled step, against the sustained bf16 peak
+    tc = prof_step.get("gemm_tc")
+    if tc and tc.get("issued"):
+        pk = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0))
+        ach = tc["issued"] / (tc["ms"] / 1e3) / 1e12
+        out["tensor"] = {"kernel": "gemm_tc", "bound": "tensor", "achieved": ach, "peak": pk,
+                         "unit": "TFLOP/s (bf16 issued)", "frac": ach / pk,
+                         "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)",
+                         "fp64_equivalent_tflops": tc["flops"] / (tc["ms"] / 1e3) / 1e12,
+                         "launches": tc["launches"], "avg_launch_ms": tc["ms"] / tc["launches"],
+                         "events_from": "one profiled step after the timed region (events around each launch)"}
+    return out
 
 
 def _dtype_label(prec: str) -> str:
@@ -356,7 +404,8 @@ def bench_ours(args, rank: int, world: int, dist):
     else:
         acc = {"note": "FP64 path; parity with the reference pinned at <=1e-12 by the test suite"}
 
-    roof = None if args.bare else _roofline(torch, prof)
+    roof = None if args.bare else _roofline(torch, prof, prec, b, a)
+    per_call = None if args.bare else _per_call_ms(torch, sg, A, A0, prec)
 
     # end to end through the public API with pinned host arrays
     e2e = None
@@ -383,7 +432,7 @@ def bench_ours(args, rank: int, world: int, dist):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        n_s = args.cpu_sample_blocks
+        n_s = max(2, min(args.cpu_sample_blocks, n))  # the reference arm's sample
         v, dt = run_oracle_sample(n_s, b, a)
         cpu = {"value": v, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
                "sample": f"{n_s} of {n} diagonal blocks (b={b}, a={a}), {dt:.1f} s, OpenBLAS all threads"}
@@ -406,6 +455,7 @@ def bench_ours(args, rank: int, world: int, dist):
             "e2e": e2e,
             "gpu_launches": launches,
             "kernel_profile_one_step": prof[1],
+            "per_call_ms": per_call,
             "clocks": clk,
             "hbm_bytes_algorithmic_per_step": 2 * nbytes_sweep(n, b, a),
         }
@@ -424,31 +474,28 @@ def bench_ours(args, rank: int, world: int, dist):
 def bench_batched(args):
     """256 uneven matrices (n ~ U{16..256}, b in {32,64,128,256}, a in {0,4,16}),
     half float32 / half float64, 4 RHS each, in one graph launch per step:
-    pobtaf -> pobtas N/T -> pobtasi for every matrix.  Stream count from the
-    autotuner.  Value: matrices/s."""
+    pobtaf -> pobtas N/T -> pobtasi for every matrix.  Inputs from the NumPy
+    generator (``batch_shapes``; matrix i from ``generate(..., seed=i)``).
+    Stream count from the autotuner.  Value: matrices/s.  Every item's
+    outputs are compared with the single-matrix FP64 GPU path on the same
+    inputs (float32 items: their inputs promoted to float64)."""
     import torch
 
+    import serinv_gb300 as sg
     from serinv_gb300 import _lib
     from serinv_gb300.batched import BatchPlan, autotune_nstreams
-    from serinv_gb300.synthetic import generate_torch
+    from serinv_gb300.synthetic import batch_shapes, generate
 
     torch.cuda.set_device(0)
     _lib.load()
-    rng = np.random.default_rng(0)
     count = args.batch_count
-    shapes = []
-    for i in range(count):
-        n = int(rng.integers(16, 257))
-        b = int(rng.choice([32, 64, 128, 256]))
-        a = int(rng.choice([0, 4, 16]))
-        dt = torch.float32 if i < count // 2 else torch.float64
-        shapes.append((n, b, a, dt))
+    shapes = batch_shapes(count, 0)
     src, rhs0 = [], []
     tot_flops = 0.0
     for i, (n, b, a, dt) in enumerate(shapes):
-        D, Lo, Ar, T, B = generate_torch(n, b, a, 4, seed=i, dtype=dt)
-        src.append((D, Lo, Ar, T))
-        rhs0.append(B)
+        m = generate(n, b, a, 4, seed=i, dtype=dt)
+        src.append(tuple(torch.from_numpy(x).cuda() for x in m.arrays()))
+        rhs0.append(torch.from_numpy(m.B).cuda())
         f = flops(n, b, a, 4)
         tot_flops += f["pobtaf"] + f["pobtasi"] + f["pobtas"]
     work = [tuple(x.clone() for x in m) for m in src]
@@ -483,13 +530,34 @@ def bench_batched(args):
         times.append(e0.elapsed_time(e1) / 1e3)
     t = float(np.median(times))
     bad = int((plan.info() != 0).sum())
+
+    # accuracy: the last replay's outputs against the single-matrix FP64 path
+    worst = {"float32": 0.0, "float64": 0.0}
+    for (d, x), m_src, r_src in zip(zip(work, rhs), src, rhs0):
+        ref = [y.to(torch.float64).clone() for y in m_src]
+        xr = r_src.to(torch.float64).clone()
+        sg.pobtaf(*ref)
+        L = [y.clone() for y in ref]
+        sg.pobtas(*L, xr, trans="N")
+        sg.pobtas(*L, xr, trans="T")
+        sg.pobtasi(*ref)
+        e = 0.0
+        for g, r_ in list(zip(d, ref)) + [(x, xr)]:
+            if r_.numel():
+                nr = float(torch.linalg.norm(r_))
+                e = max(e, float(torch.linalg.norm(g.to(torch.float64) - r_)) / max(nr, 1e-300))
+        key = "float32" if d[0].dtype == torch.float32 else "float64"
+        worst[key] = max(worst[key], e)
     line = {"metric": "batched BTA matrices/s (256 uneven, f32+f64, pobtaf+pobtas+pobtasi, 1 graph launch)",
             "value": count / t, "unit": "matrices/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t * 1e3, "higher_is_better": True, "tflops": tot_flops / t / 1e12,
             "dtype": "half f32, half " + ("f64 mixed" if args.batch_precision == "mixed" else "f64"),
-            "data": "synthetic (torch generator, seed i for matrix i)",
+            "data": "synthetic (NumPy generator, seed i for matrix i)",
             "config": {"workload": "batch of 256 uneven BTA matrices", "nstreams": ns,
                        "autotune_s": tune_s, "not_spd": bad},
+            "max_rel_err_vs_single_fp64": {**worst, "vs": "single-matrix FP64 GPU path on the same inputs, "
+                                                         "max over items of the relative Frobenius error of "
+                                                         "each output stack and the solution"},
             "gpu_launches": kernels_per_graph}
     print(json.dumps(line), flush=True)
 

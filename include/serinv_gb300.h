@@ -72,6 +72,11 @@ extern "C" {
  * error ~2^-(7S+1) of the row maxima; measured on pobtaf+pobtasi at
  * n=512, b=512, a=64: S=5 ~4e-9, S=6 ~3e-11, S=7 ~3e-13 relative.
  * FP64 storage only.
+ * Bits 16-23 (3..7; 0 = S) set a separate slice count Si for the products
+ * with an explicit triangular inverse -- pobtaf's rows-below-the-diagonal
+ * times L_ii^{-T}, pobtasi's batched inversions and its products with
+ * L_ii^{-1} -- whose error grows with the condition of L_ii:
+ * SGB_PREC_MIXED | (S << 8) | (Si << 16).
  * The first 4 bytes of the workspace receive a device status word (0, or
  * SGB_ERR_TIMEOUT if a bounded tensor-core wait gave up).                 */
 #define SGB_PREC_MIXED  1
@@ -232,6 +237,10 @@ int sgb_pobtas_refine(const sgb_bta* A, const sgb_bta* L, void* rhs, int64_t nrh
  * first call before any stream capture.  All calls share the array: calls
  * that overlap on the GPU race and must be serialised by the caller.
  * No cudaMalloc, cudaFree or other allocating routine is called.
+ * info (device int32, may be NULL) reports as sgb_pobtaf's does, plus one
+ * code of its own: -SGB_ERR_TIMEOUT if a bounded device wait gave up (the
+ * status word that sgb_pobtaf leaves in the caller's workspace is private
+ * here).  With info NULL a timeout is not reported.
  */
 int sgb_pobtaf_noalloc(const sgb_bta* m, int factorize_last_block, int32_t* info, void* stream);
 size_t sgb_pobtaf_noalloc_scratch_bytes(void);
@@ -294,6 +303,16 @@ int sgb_batch_plan_destroy(sgb_batch_plan* plan);
 /* Number of kernels this library has launched since it was loaded. */
 long long sgb_launch_count(void);
 
+/* Poll limit of the bounded device waits (the column-block kernel's
+ * counters, barriers and staged hand-offs, the tensor-core pipeline's
+ * mbarriers); default 2^22 polls, about a second.  Sets the limit for
+ * launches made after the call (polls >= 0) and returns the previous one;
+ * polls < 0 only queries.  A test hook: a limit of 0 makes every wait that
+ * does not find its condition already met give up at once, so the timeout
+ * path (status word SGB_ERR_TIMEOUT, every CTA leaving, tensor memory
+ * freed) runs without any real hang.  Process-wide; not for production. */
+long long sgb_debug_spin_limit(long long polls);
+
 /* Enable (1) or disable (0) per-launch CUDA-event timing; clears records. */
 int sgb_profile_enable(int on);
 
@@ -306,6 +325,12 @@ int sgb_profile_enable_classes(unsigned mask);
  * milliseconds between the events bracketing each launch, and algorithmic
  * flops (useful multiply-adds x 2).  Synchronises on the recorded events. */
 int sgb_profile_read(int kclass, long long* launches, double* ms, double* flops);
+
+/* Arithmetic the hardware issued over the same recorded launches, where it
+ * differs from the algorithmic flops: for SGB_KCLASS_GEMM_TC the bf16
+ * multiply-adds x 2 of every slice product the MMA warp issues (padding,
+ * K splits and all S(S+1)/2 slice pairs included); 0 for other classes. */
+int sgb_profile_read_issued(int kclass, double* issued);
 
 #ifdef __cplusplus
 }

@@ -36,12 +36,21 @@ PRECISIONS = {"native": SGB_PREC_NATIVE, "fp64": SGB_PREC_NATIVE, "mixed": SGB_P
 
 
 def precision_code(precision) -> int:
-    """'fp64' / 'native' -> native; 'mixed' -> 6 slices; 'mixed:S' -> S slices (3..7)."""
+    """'fp64' / 'native' -> native; 'mixed' -> 6 slices; 'mixed:S' -> S slices
+    (3..7); 'mixed:S:Si' -> S slices, and Si for the products with an
+    explicit triangular inverse (the accuracy lever at ill conditioning)."""
     if isinstance(precision, str) and precision.startswith("mixed:"):
-        S = int(precision.split(":", 1)[1])
-        if not 3 <= S <= 7:
-            raise ValueError(f"slice count must be in 3..7, got {S}")
-        return SGB_PREC_MIXED | (S << 8)
+        parts = precision.split(":")[1:]
+        if not 1 <= len(parts) <= 2:
+            raise ValueError(f"precision must be 'mixed:S' or 'mixed:S:Si', got {precision!r}")
+        counts = [int(x) for x in parts]
+        for c in counts:
+            if not 3 <= c <= 7:
+                raise ValueError(f"slice count must be in 3..7, got {c}")
+        code = SGB_PREC_MIXED | (counts[0] << 8)
+        if len(counts) == 2:
+            code |= counts[1] << 16
+        return code
     if precision not in PRECISIONS:
         raise ValueError(f"precision must be 'fp64', 'mixed' or 'mixed:S', got {precision!r}")
     return PRECISIONS[precision]
@@ -125,10 +134,12 @@ _SIGNATURES = {
     "sgb_batch_info": (ctypes.c_void_p, [ctypes.c_void_p]),
     "sgb_batch_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "sgb_launch_count": (ctypes.c_longlong, []),
+    "sgb_debug_spin_limit": (ctypes.c_longlong, [ctypes.c_longlong]),
     "sgb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "sgb_profile_enable_classes": (ctypes.c_int, [ctypes.c_uint]),
     "sgb_profile_read": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "sgb_profile_read_issued": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
 }
 
 KCLASS = {"gemm": 0, "potrf_tile": 1, "trtri_tile": 2, "gemm_tc": 3, "split": 4, "panel": 5, "embed": 6}
@@ -165,6 +176,12 @@ def exported_symbols():
     return list(_SIGNATURES)
 
 
+def spin_limit(polls: int = -1) -> int:
+    """Poll limit of the bounded device waits; sets it when polls >= 0 and
+    returns the previous value (a test hook for the timeout path)."""
+    return int(load().sgb_debug_spin_limit(int(polls)))
+
+
 def launch_count() -> int:
     """Kernels launched by the library since it was loaded."""
     return int(load().sgb_launch_count())
@@ -188,7 +205,11 @@ def profile_read() -> dict:
         fl = ctypes.c_double(0)
         raise_for(lib.sgb_profile_read(k, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(fl)), "profile")
         if n.value:
+            iss = ctypes.c_double(0)
+            raise_for(lib.sgb_profile_read_issued(k, ctypes.byref(iss)), "profile")
             out[name] = {"launches": n.value, "ms": ms.value, "flops": fl.value}
+            if iss.value:
+                out[name]["issued"] = iss.value
     return out
 
 

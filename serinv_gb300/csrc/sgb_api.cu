@@ -57,8 +57,22 @@ int parse_precision(int precision, int dtype) {
     int S = (precision >> 8) & 0xff;
     if (S == 0) S = kDefaultSlices;
     if (S < 3 || S > 7) return -SGB_ERR_ARG;
+    const int Si = (precision >> 16) & 0xff;
+    if ((Si != 0 && (Si < 3 || Si > 7)) || (precision >> 24) != 0) return -SGB_ERR_ARG;
     if (dtype != SGB_F64) return -SGB_ERR_UNSUPPORTED;
     return S;
+}
+
+// Slice count of the products with an explicit triangular inverse (the
+// rows below a diagonal block times L_ii^{-T} in pobtaf; the batched
+// inversions and the G, H, P products of pobtasi): bits 16-23 of the
+// precision argument, 0 = the same as S.  Their error grows with the
+// condition of L_ii, so a larger count there buys accuracy at ill
+// conditioning for a small share of the time.
+int parse_inv_slices(int precision, int S) {
+    if (S <= 0) return 0;
+    const int Si = (precision >> 16) & 0xff;
+    return Si == 0 ? S : Si;
 }
 
 // Everything a block sweep needs besides the matrix: precision and the
@@ -165,13 +179,14 @@ struct Carve {
 template <typename T>
 struct PobtafWs {
     size_t status, bar, tinv, tc, tc_bytes, xinv, total;
-    PobtafWs(const sgb_bta* m, int S = 0) {
+    PobtafWs(const sgb_bta* m, int S = 0, int Si = 0) {
         Carve c;
         status = c.take(256);
         bar = c.take(256);
         tinv = c.take(sizeof(T) * (10 * kTile * kTile + 9 * kTile));  // column-block kernel scratch
         const int64_t mx = m->b > m->a ? m->b : m->a;
-        tc_bytes = S ? tc_bound(S, mx, m->b, 3) : 0;
+        const int Sm = Si > S ? Si : S;
+        tc_bytes = S ? tc_bound(Sm, mx, m->b, 3) : 0;
         tc = c.take(tc_bytes);
         // mixed precision only: L_ii^{-T} of the current diagonal block
         xinv = c.take(S ? sizeof(T) * m->b * m->b : 0);
@@ -199,12 +214,13 @@ template <typename T>
 struct PobtasiWs {
     size_t status, linv, linv_tip, trtri, gh, tc, tc_bytes, total;
     int64_t chunk;
-    PobtasiWs(const sgb_bta* m, int S = 0) {
+    PobtasiWs(const sgb_bta* m, int S = 0, int Si = 0) {
         const int64_t n = m->n, b = m->b, a = m->a;
         chunk = n < kSiChunk ? (n > 0 ? n : 1) : kSiChunk;
         Carve c;
         status = c.take(256);
         tc_bytes = 0;
+        if (Si > S) S = Si;  // scratch for the larger of the two slice counts
         if (S) {
             const int64_t kba = ceil_div(b, 32) * 32 + ceil_div(a, 32) * 32;
             const int64_t tb = chunk < kSiTcBatch ? chunk : kSiTcBatch;
@@ -409,20 +425,22 @@ struct HostLink {
 //   [D_i; Lo_i; Ar_i] <- blocked Cholesky of the column block  (:117-139)
 //   D_{i+1} -= Lo_i Lo_i^T, Ar_{i+1} -= Ar_i Lo_i^T, T -= Ar_i Ar_i^T  (:143-159)
 template <typename T>
-int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int32_t* info, cudaStream_t s,
+int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* ws, int32_t* info, cudaStream_t s,
                HostLink* hl = nullptr, T* xall = nullptr, bool* xall_filled = nullptr) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
     T* Ar = (T*)m->arrow;
     T* Tp = (T*)m->tip;
-    PobtafWs<T> L(m, S);
+    PobtafWs<T> L(m, S, Si);
     T* tinv = (T*)((char*)ws + L.tinv);
     Ctx cx;
     cx.slices = S;
     cx.tc = (char*)ws + L.tc;
     cx.tc_bytes = L.tc_bytes;
     cx.status = (int32_t*)((char*)ws + L.status);
+    Ctx cxi = cx;  // products with L_ii^{-T}
+    cxi.slices = Si;
     const int64_t bb = b * b, ab = a * b;
     T* Xinv0 = (T*)((char*)ws + L.xinv);
 
@@ -468,7 +486,7 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
                     p.ldc = r.ld;
                     pr[np++] = p;
                 }
-                if (np) SGB_TRY(run_gemm<T>(cx, pr, np, s));
+                if (np) SGB_TRY(run_gemm<T>(cxi, pr, np, s));
                 return SGB_OK;
             }
             if (e != cudaErrorNotSupported) return cuda_fail(e);
@@ -578,20 +596,22 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, void* ws, int3
 // Lo_i and Ar_i are dead once G_i, H_i, P_i exist, so P_i is formed in the
 // diagonal block itself and the outputs overwrite the factor in place.
 template <typename T>
-int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaStream_t s,
+int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws, cudaStream_t s,
                 HostLink* hl = nullptr, const T* xall = nullptr) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
     T* Ar = (T*)m->arrow;
     T* Tp = (T*)m->tip;
-    PobtasiWs<T> W(m, S);
+    PobtasiWs<T> W(m, S, Si);
     char* base = (char*)ws;
     Ctx cx;
     cx.slices = S;
     cx.tc = base + W.tc;
     cx.tc_bytes = W.tc_bytes;
     cx.status = (int32_t*)(base + W.status);
+    Ctx cxi = cx;  // the inversions and the products with L_ii^{-1}
+    cxi.slices = Si;
     T* Linv = (T*)(base + W.linv);
     T* Ltinv = (T*)(base + W.linv_tip);
     T* trs = (T*)(base + W.trtri);
@@ -604,13 +624,13 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
     }
     if (invert_last_block && a) {
         // X_T = L_T^{-T} L_T^{-1}  (:115-119)
-        SGB_TRY(trtri_run<T>(cx, Tp, a, 1, Ltinv, trs, s));
+        SGB_TRY(trtri_run<T>(cxi, Tp, a, 1, Ltinv, trs, s));
         GemmProb<T> p = prob<T>();
         p.M = p.N = (int32_t)a;
         set_term<T>(p, 0, Ltinv, a, 1, Ltinv, a, 0, a, KM_GE_M0);
         p.Cout = Tp;
         p.ldc = a;
-        SGB_TRY(run_gemm<T>(cx, &p, 1, s));
+        SGB_TRY(run_gemm<T>(cxi, &p, 1, s));
     }
     if (hl) SGB_TRY(hl->give_tip());
 
@@ -621,7 +641,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
         const int64_t lo = hi > W.chunk ? hi - W.chunk : 0;
         if (hl) SGB_TRY(hl->need(lo, s));
         // with xall the inverses exist already, as L_jj^{-T}: operands are read transposed
-        if (!xall) SGB_TRY(trtri_run<T>(cx, D + lo * bb, b, hi - lo, Linv, trs, s));
+        if (!xall) SGB_TRY(trtri_run<T>(cxi, D + lo * bb, b, hi - lo, Linv, trs, s));
         for (int64_t j0 = lo; j0 < hi; j0 += tcb) {
             const int64_t jn = (hi - j0) < tcb ? (hi - j0) : tcb;
             const int64_t ng = (j0 + jn <= n - 1) ? jn : (n - 1 - j0);  // blocks with a Lo_j
@@ -667,7 +687,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, void* ws, cudaSt
                 p.strideC = bb;
                 pr[np++] = p;
             }
-            SGB_TRY(run_gemm<T>(cx, pr, np, s));
+            SGB_TRY(run_gemm<T>(cxi, pr, np, s));
         }
         for (int64_t i = hi - 1; i >= lo; --i) {
             const bool has_next = i < n - 1;
@@ -1213,7 +1233,8 @@ int plan_item(const sgb_bta* m, int ops, int precision, void* rhs, int64_t nrhs,
     if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
     SGB_TRY(cudaMemsetAsync(w, 0, sizeof(int32_t), s));  // status word
     bool filled = false;
-    if ((rc = pobtaf_run<double>(m, 1, S, w, info, s, nullptr, xall, &filled))) return rc;
+    const int Si = parse_inv_slices(precision, S);
+    if ((rc = pobtaf_run<double>(m, 1, S, Si, w, info, s, nullptr, xall, &filled))) return rc;
     const double* xa = filled ? xall : nullptr;
     if ((ops & SGB_OP_POBTAS) && nrhs > 0) {
         sgb_pobtas_workspace_size(m, nrhs, precision, &need);
@@ -1225,7 +1246,7 @@ int plan_item(const sgb_bta* m, int ops, int precision, void* rhs, int64_t nrhs,
     if (ops & SGB_OP_POBTASI) {
         sgb_pobtasi_workspace_size(m, precision, &need);
         if ((rc = check_ws(w, wb, need))) return rc;
-        rc = pobtasi_run<double>(m, 1, S, w, s, nullptr, xa);
+        rc = pobtasi_run<double>(m, 1, S, Si, w, s, nullptr, xa);
     }
     return rc;
 }
@@ -1264,7 +1285,8 @@ int sgb_pobtaf_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
     const int S = parse_precision(precision, m->dtype);
     if (S < 0) return -S;
     if (!bytes) return SGB_ERR_ARG;
-    *bytes = m->dtype == SGB_F64 ? PobtafWs<double>(m, S).total : PobtafWs<float>(m, S).total;
+    const int Si = parse_inv_slices(precision, S);
+    *bytes = m->dtype == SGB_F64 ? PobtafWs<double>(m, S, Si).total : PobtafWs<float>(m, S, Si).total;
     return SGB_OK;
 }
 
@@ -1275,7 +1297,8 @@ int sgb_pobtasi_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
     const int S = parse_precision(precision, m->dtype);
     if (S < 0) return -S;
     if (!bytes) return SGB_ERR_ARG;
-    *bytes = m->dtype == SGB_F64 ? PobtasiWs<double>(m, S).total : PobtasiWs<float>(m, S).total;
+    const int Si = parse_inv_slices(precision, S);
+    *bytes = m->dtype == SGB_F64 ? PobtasiWs<double>(m, S, Si).total : PobtasiWs<float>(m, S, Si).total;
     return SGB_OK;
 }
 
@@ -1367,8 +1390,9 @@ int sgb_pobtaf(const sgb_bta* m, int factorize_last_block, int precision, void* 
     cudaStream_t s = (cudaStream_t)stream;
     if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
     SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
-    if (m->dtype == SGB_F64) return pobtaf_run<double>(m, factorize_last_block, S, workspace, info, s);
-    return pobtaf_run<float>(m, factorize_last_block, S, workspace, info, s);
+    const int Si = parse_inv_slices(precision, S);
+    if (m->dtype == SGB_F64) return pobtaf_run<double>(m, factorize_last_block, S, Si, workspace, info, s);
+    return pobtaf_run<float>(m, factorize_last_block, S, Si, workspace, info, s);
 }
 
 int sgb_pobtasi(const sgb_bta* m, int invert_last_block, int precision, void* workspace, size_t workspace_bytes,
@@ -1385,8 +1409,9 @@ int sgb_pobtasi(const sgb_bta* m, int invert_last_block, int precision, void* wo
     if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
-    if (m->dtype == SGB_F64) return pobtasi_run<double>(m, invert_last_block, S, workspace, s);
-    return pobtasi_run<float>(m, invert_last_block, S, workspace, s);
+    const int Si = parse_inv_slices(precision, S);
+    if (m->dtype == SGB_F64) return pobtasi_run<double>(m, invert_last_block, S, Si, workspace, s);
+    return pobtasi_run<float>(m, invert_last_block, S, Si, workspace, s);
 }
 
 int sgb_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char trans, int partial, int precision,
@@ -1575,8 +1600,10 @@ int sgb_pobtaf_host(const sgb_bta* host, const sgb_bta* dev, int factorize_last_
     hl.d = dev;
     hl.ascending = true;
     hl.es = dev->dtype == SGB_F64 ? 8 : 4;
-    if (dev->dtype == SGB_F64) return pobtaf_run<double>(dev, factorize_last_block, S, workspace, info, s, &hl);
-    return pobtaf_run<float>(dev, factorize_last_block, S, workspace, info, s, &hl);
+    const int Si = parse_inv_slices(precision, S);
+    if (dev->dtype == SGB_F64)
+        return pobtaf_run<double>(dev, factorize_last_block, S, Si, workspace, info, s, &hl);
+    return pobtaf_run<float>(dev, factorize_last_block, S, Si, workspace, info, s, &hl);
 }
 
 int sgb_pobtasi_host(const sgb_bta* host, const sgb_bta* dev, int invert_last_block, int precision,
@@ -1595,8 +1622,9 @@ int sgb_pobtasi_host(const sgb_bta* host, const sgb_bta* dev, int invert_last_bl
     hl.d = dev;
     hl.ascending = false;
     hl.es = dev->dtype == SGB_F64 ? 8 : 4;
-    if (dev->dtype == SGB_F64) return pobtasi_run<double>(dev, invert_last_block, S, workspace, s, &hl);
-    return pobtasi_run<float>(dev, invert_last_block, S, workspace, s, &hl);
+    const int Si = parse_inv_slices(precision, S);
+    if (dev->dtype == SGB_F64) return pobtasi_run<double>(dev, invert_last_block, S, Si, workspace, s, &hl);
+    return pobtasi_run<float>(dev, invert_last_block, S, Si, workspace, s, &hl);
 }
 
 }  // extern "C"

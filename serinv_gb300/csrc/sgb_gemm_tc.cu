@@ -56,7 +56,7 @@ constexpr int kMaxTcProbs = 4;
 constexpr int64_t kTcSmCount = 148;  // CTAs one launch should keep busy (152 SMs)
 constexpr int kTcMaxSplit = 4;      // CTAs per cluster of a K-split tile
 constexpr int kMaxSplitJobs = 2 * kMaxTcProbs;  // probs x operands
-constexpr long long kSpinLimit = 1ll << 22;         // bounded mbarrier waits (~1 s)
+constexpr long long kSpinLimit = 1ll << 22;         // bounded drain waits after an error (~1 s)
 
 // ---------------------------------------------------------------- split
 
@@ -280,6 +280,7 @@ struct TcLaunch {
     int32_t np;
     int32_t ks;    // CTAs per output tile (a cluster), each over a K slice
     int32_t* err;  // set to SGB_ERR_TIMEOUT if a bounded wait gave up
+    long long spin;  // poll limit of the pipeline's mbarrier waits
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -321,9 +322,9 @@ __device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait: returns false if the phase did not complete in time.
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
-    for (long long i = 0; i < kSpinLimit; ++i)
+// Bounded wait: returns false if the phase did not complete in `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, long long limit) {
+    for (long long i = 0; i < limit; ++i)
         if (mbar_try(addr, parity)) return true;
     return false;
 }
@@ -469,7 +470,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
     uint64_t* empty = full + NS;
     uint64_t* done = empty + NS;
     uint32_t* tmem_slot = (uint32_t*)(done + 1);
-    int* flags = (int*)(tmem_slot + 1);  // [0] error seen
+    int* flags = (int*)(tmem_slot + 1);  // [0] error seen, [1] K blocks the producer issued
 
     const int ks = L.ks;  // CTAs of this tile's cluster, one K slice each
     const uint32_t rank = ks > 1 ? cluster_rank() : 0u;
@@ -506,6 +507,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         }
         mbar_init(smem_u32(done), 1);
         flags[0] = 0;
+        flags[1] = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -528,12 +530,14 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
     if (warp == 4) {
         // producer
         if (lane == 0) {
+            int issued = 0;
             for (int kb = 0; kb < nkb; ++kb) {
                 const int st = kb % NS, round = kb / NS;
-                if (kb >= NS && !mbar_wait(smem_u32(&empty[st]), (uint32_t)((round - 1) & 1))) {
+                if (kb >= NS && !mbar_wait(smem_u32(&empty[st]), (uint32_t)((round - 1) & 1), L.spin)) {
                     atomicExch(&flags[0], 1);
                     break;
                 }
+                issued = kb + 1;
                 const uint32_t fb = smem_u32(&full[st]);
                 mbar_expect_tx(fb, (uint32_t)SM::kStage);
                 const uint32_t sA = sbase + st * SM::kStage, sB = sA + SM::kA;
@@ -545,6 +549,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
                              BN * TC_BK * 2, fb);
                 }
             }
+            flags[1] = issued;
         }
     } else if (warp == 5) {
         // MMA issuer
@@ -553,7 +558,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
             uint32_t inited = 0;
             for (int kb = 0; kb < nkb; ++kb) {
                 const int st = kb % NS, round = kb / NS;
-                if (!mbar_wait(smem_u32(&full[st]), (uint32_t)(round & 1)) || flags[0]) {
+                if (!mbar_wait(smem_u32(&full[st]), (uint32_t)(round & 1), L.spin) || flags[0]) {
                     atomicExch(&flags[0], 1);
                     break;
                 }
@@ -588,7 +593,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
     // threads on consecutive columns, so global loads and stores coalesce.
     bool ok = true;
     if (warp < 4) {
-        if (!mbar_wait(smem_u32(done), 0)) ok = false;
+        if (!mbar_wait(smem_u32(done), 0, L.spin)) ok = false;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
     const bool all_ok = !__syncthreads_or(!ok || flags[0] != 0);
@@ -618,7 +623,11 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         lo = lo - (h2 - hi);
         hi = h2;
     };
+    // a row of op(A) or column of op(B) holding an Inf or NaN (biased
+    // exponent 2047: its digits carry no value) makes the element NaN, as
+    // the FP64 product would; a zero row or column otherwise gives 0
     auto finish = [&](float hi, float lo, int eAm, int eBn) -> double {
+        if (eAm == 0x7ff || eBn == 0x7ff) return __longlong_as_double(0x7ff8000000000000ll);
         if (eAm == 0 || eBn == 0) return 0.0;
         return scale_pow2(f32_to_f64(hi) + f32_to_f64(lo), eAm + eBn - 2058);
     };
@@ -749,12 +758,13 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         }
     }
     if (!all_ok && tid == 0) {
-        // drain (bounded): the final commit, then any stage still being filled
-        mbar_wait(smem_u32(done), 0);
-        for (int i = 0; i < NS; ++i) {
-            mbar_wait(smem_u32(&full[i]), 0);
-            mbar_wait(smem_u32(&full[i]), 1);
-        }
+        // drain (bounded by the fixed limit, not the pipeline's): the final
+        // commit, then the last round of bulk copies issued into each stage
+        // (earlier rounds completed before their stage was refilled)
+        mbar_wait(smem_u32(done), 0, kSpinLimit);
+        const int issued = flags[1];
+        for (int kb = issued > NS ? issued - NS : 0; kb < issued; ++kb)
+            mbar_wait(smem_u32(&full[kb % NS]), (uint32_t)((kb / NS) & 1), kSpinLimit);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -858,6 +868,7 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
     TcLaunch TL;
     memset(&TL, 0, sizeof(TL));
     TL.err = err;
+    TL.spin = spin_limit();
     char* base = (char*)ws;
     size_t off = 0;
     int64_t split_ctas = 0, gemm_tiles = 0;
@@ -998,6 +1009,18 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
     }
     double fl = 0.0;
     for (int i = 0; i < np; ++i) fl += useful_flops<double>(probs[i]);
+    // bf16 flops the MMA warps issue: every tile that runs (above-diagonal
+    // tiles of a lower-only product exit) times its padded K times the
+    // S(S+1)/2 slice pairs
+    double issued = 0.0;
+    for (int i = 0; i < TL.np; ++i) {
+        const TcProb& tp = TL.p[i];
+        int64_t run = 0;
+        for (int mt = 0; mt < tp.tiles_m; ++mt)
+            for (int nt = 0; nt < tp.tiles_n; ++nt)
+                if (!(tp.lower_only && nt * bn >= mt * TC_BM + TC_BM)) ++run;
+        issued += 2.0 * run * tp.batch * (double)TC_BM * bn * tp.Kpad * (S * (S + 1) / 2);
+    }
     cudaError_t e = tc_prepare();
     if (e != cudaSuccess) return e;
     prof_before(s, SGB_KCLASS_GEMM_TC);
@@ -1018,7 +1041,7 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
             default: e = launch_tc<7, 32>(TL, (int)gemm_tiles, s); break;
         }
     }
-    prof_after(SGB_KCLASS_GEMM_TC, s, fl);
+    prof_after(SGB_KCLASS_GEMM_TC, s, fl, issued);
     return e;
 }
 

@@ -184,11 +184,17 @@ int cx_pobtasi(const sgb_bta* m, int ilb, int precision, void* ws, size_t ws_byt
 int cx_pobtas(const sgb_bta* m, void* rhs, int64_t nrhs, int64_t ldb, char trans, int partial, int precision,
               void* ws, size_t ws_bytes, cudaStream_t s, void* buffer);
 
+// Poll limit of the bounded device waits (sgb_prof.cu): 2^22 unless a test
+// lowered it through sgb_debug_spin_limit.
+long long spin_limit();
+
 // Launch accounting (sgb_prof.cu): call prof_before just before and
 // prof_after just after every kernel launch.
 void prof_before(cudaStream_t s, int kclass = -1);
 // True while `s` is being captured into a graph.
 bool capturing(cudaStream_t s);
-void prof_after(int kclass, cudaStream_t s, double flops);
+// `issued`: arithmetic the hardware performs for the launch when it differs
+// from the algorithmic flops (the tensor-core kernel: bf16 slice products).
+void prof_after(int kclass, cudaStream_t s, double flops, double issued = 0.0);
 
 }  // namespace sgb

@@ -10,11 +10,29 @@
 //
 // The array costs kStaticScratchBytes of device memory on every GPU that
 // loads this library, for the lifetime of the process.  All calls share it
-// and it keeps the previous call's contents; pobtaf overwrites every byte it
-// reads before reading it (the 32 x 32 tile inverse), so nothing needs
-// clearing.  Two calls that overlap on the GPU (different streams, or
-// different host threads on one device) race on the array and must be
-// serialised by the caller.
+// and it keeps the previous call's contents.  It holds pobtaf's workspace,
+// whose three regions are each made safe to reuse by the call itself:
+//
+//   * the status word (first 4 bytes): cleared by a memset at the start of
+//     every call;
+//   * the barrier and column counters of the persistent column-block
+//     kernel: cleared by a memset before every launch of that kernel;
+//   * the column-block kernel's staging buffers and published columns: the
+//     factorizer CTA resets every staging element to a sentinel on entry,
+//     before any other CTA can see a column counter move, and every
+//     published column is written before its counter is raised; the
+//     launch-based tile sweep (small blocks) writes its 32 x 32 tile
+//     scratch before reading it.
+//
+// So leftover contents from an earlier call are never read as data.  Two
+// calls that overlap on the GPU (different streams, or different host
+// threads on one device) race on the array and must be serialised by the
+// caller.
+//
+// A bounded wait that gives up inside the column-block kernel sets the
+// status word; that word lives in the private array, so after the sweep a
+// one-thread kernel copies a non-zero status into the caller's `info` word
+// as -SGB_ERR_TIMEOUT (info > 0 keeps its meaning: the failing pivot row).
 #include <mutex>
 
 #include "sgb_internal.cuh"
@@ -48,6 +66,13 @@ int scratch_address(void** out) {
     return SGB_OK;
 }
 
+// A timeout recorded in the private status word becomes -SGB_ERR_TIMEOUT in
+// the caller's info word.
+__global__ void k_status_to_info(const int32_t* status, int32_t* info) {
+    const int32_t s = *status;
+    if (s != 0) *info = -s;
+}
+
 }  // namespace
 
 extern "C" {
@@ -62,7 +87,14 @@ int sgb_pobtaf_noalloc(const sgb_bta* m, int factorize_last_block, int32_t* info
     void* scratch = nullptr;
     rc = scratch_address(&scratch);
     if (rc != SGB_OK) return rc;
-    return sgb_pobtaf(m, factorize_last_block, SGB_PREC_NATIVE, scratch, kStaticScratchBytes, info, stream);
+    rc = sgb_pobtaf(m, factorize_last_block, SGB_PREC_NATIVE, scratch, kStaticScratchBytes, info, stream);
+    if (rc != SGB_OK || info == nullptr) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    sgb::prof_before(s);
+    k_status_to_info<<<1, 1, 0, s>>>((const int32_t*)scratch, info);
+    const cudaError_t e = cudaGetLastError();
+    sgb::prof_after(-1, s, 0.0);
+    return e == cudaSuccess ? SGB_OK : sgb::record_cuda_error(e);
 }
 
 }  // extern "C"

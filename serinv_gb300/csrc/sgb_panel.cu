@@ -52,7 +52,6 @@ namespace sgb {
 namespace {
 
 constexpr int NT = 256;
-constexpr long long kBarrierSpin = 1ll << 22;
 constexpr int kNH = 8;                 // helper CTAs of the next diagonal tile
 constexpr int kHelpRows = kTile / kNH;  // rows of a tile-row per helper
 constexpr int kInv = kNH + 1;           // the L writer CTA
@@ -76,6 +75,7 @@ struct PanelArgs {
     unsigned* bar;    // [0] F, [1] I, [4] barrier B, [6] barrier C, [8] columns of M
                       // published; zero at launch
     int32_t* status;  // SGB_ERR_TIMEOUT on a stuck wait
+    long long spin;   // poll limit of every bounded wait
 };
 
 template <typename T>
@@ -98,7 +98,7 @@ __device__ __forceinline__ bool status_bad(const int32_t* status) {
 // Arrivals are fire-and-forget reductions, so no CTA waits for an atomic's
 // return.  Returns false (on every thread of the CTA) if it timed out.
 __device__ __forceinline__ bool group_barrier(unsigned* cnt, unsigned nblocks, unsigned& epoch, int32_t* status,
-                                              int* sflag) {
+                                              int* sflag, long long spin) {
     __syncthreads();
     if (threadIdx.x == 0) {
         epoch += 1;
@@ -108,7 +108,7 @@ __device__ __forceinline__ bool group_barrier(unsigned* cnt, unsigned nblocks, u
         asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(cnt) : "memory");
         long long spins = 0;
         while ((int)(ld_acquire(cnt) - target) < 0) {
-            if (++spins > kBarrierSpin || status_bad(status)) {
+            if (++spins > spin || status_bad(status)) {
                 ok = 0;
                 atomicExch(status, SGB_ERR_TIMEOUT);
                 break;
@@ -123,12 +123,13 @@ __device__ __forceinline__ bool group_barrier(unsigned* cnt, unsigned nblocks, u
 
 // Wait until *ctr >= target (tight poll: only a few CTAs wait here); false
 // (on every thread) on a timeout or an error raised elsewhere.
-__device__ __forceinline__ bool wait_count(const unsigned* ctr, unsigned target, int32_t* status, int* sflag) {
+__device__ __forceinline__ bool wait_count(const unsigned* ctr, unsigned target, int32_t* status, int* sflag,
+                                           long long spin) {
     if (threadIdx.x == 0) {
         long long spins = 0;
         int ok = 1;
         while (ld_acquire(ctr) < target) {
-            if (++spins > kBarrierSpin || status_bad(status)) {
+            if (++spins > spin || status_bad(status)) {
                 ok = 0;
                 atomicExch(status, SGB_ERR_TIMEOUT);
                 break;
@@ -182,8 +183,8 @@ __device__ __forceinline__ T* row_ptr(const PanelArgs<T>& a, int64_t c1, int64_t
 // timeout or an error raised elsewhere.
 template <typename T>
 __device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T* rv, const unsigned* colcount,
-                                              unsigned col_base, int32_t* status, bool sleep, int unit = -1,
-                                              T* stage_row = nullptr) {
+                                              unsigned col_base, int32_t* status, bool sleep, long long spin,
+                                              int unit = -1, T* stage_row = nullptr) {
     const int tx = threadIdx.x & 31;
     T y = tx < w ? (unit >= 0 ? T(tx == unit ? 1 : 0) : ldcg(rp + tx)) : T(0);
     T r = T(0);
@@ -196,7 +197,7 @@ __device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T
                 const unsigned c = ld_acquire(colcount);
                 avail = c > col_base ? (int)(c - col_base) : 0;
                 if (avail > k) break;
-                if (++spins > kBarrierSpin || status_bad(status)) {
+                if (++spins > spin || status_bad(status)) {
                     atomicExch(status, SGB_ERR_TIMEOUT);
                     avail = -1;
                     break;
@@ -239,7 +240,8 @@ __device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T
 // arrive.  The result also goes to the staging row.  Returns false on a
 // timeout or an error raised elsewhere.
 template <typename T>
-__device__ __forceinline__ bool trsm_row_vals(T* rp, int w, const T* vc, int32_t* status, T* stage_row) {
+__device__ __forceinline__ bool trsm_row_vals(T* rp, int w, const T* vc, int32_t* status, T* stage_row,
+                                              long long spin) {
     const int tx = threadIdx.x & 31;
     T y = tx < w ? ldcg(rp + tx) : T(0);
     T r = T(0);
@@ -255,7 +257,7 @@ __device__ __forceinline__ bool trsm_row_vals(T* rp, int w, const T* vc, int32_t
         for (int u = 0; u < 8; ++u)
             if (navail == u && u < nb && __all_sync(0xffffffffu, raw[u] != Staged<T>::kSentinel)) navail = u + 1;
         if (navail == 0) {
-            if (++rounds > kBarrierSpin || ((rounds & 63) == 0 && status_bad(status))) {
+            if (++rounds > spin || ((rounds & 63) == 0 && status_bad(status))) {
                 atomicExch(status, SGB_ERR_TIMEOUT);
                 return false;
             }
@@ -273,7 +275,7 @@ __device__ __forceinline__ bool trsm_row_vals(T* rp, int w, const T* vc, int32_t
             const T* dp[1] = {vc + kTile * kTile + tx};
             const bool want[1] = {true};
             T dv[1];
-            if (!stage_take<T, 1>(dp, want, dv, kBarrierSpin, status)) atomicExch(status, SGB_ERR_TIMEOUT);
+            if (!stage_take<T, 1>(dp, want, dv, spin, status)) atomicExch(status, SGB_ERR_TIMEOUT);
             d = dv[0];
             r = rsq<T>(d);
         }
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         for (int64_t p = 0; p < nt; ++p) {
             const int64_t c0 = p * kTile;
             const int w = tile_w(p);
-            if (p >= 3 && !wait_count(I, (unsigned)(p - 2), a.status, &S.flag)) return;  // buffer p % 3 free
+            if (p >= 3 && !wait_count(I, (unsigned)(p - 2), a.status, &S.flag, a.spin)) return;  // buffer p % 3 free
             const int buf = (int)(p % 3);
             // tile p >= 1 arrives by value from the helpers (their update
             // with column block p-1); tile-row staging p-1 is then free
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                              dg + buf * kTile, rg + buf * kTile, CC, (unsigned)(p * kTile),
                              p >= 1 ? stT + (p & 1) * kTile * kTile : nullptr,
                              p >= 1 ? stL + ((p - 1) & 1) * kTile * kTile : nullptr, a.status, stV + (p % 3) * kVc,
-                             p >= 1 ? stV + ((p - 1) % 3) * kVc : nullptr);
+                             p >= 1 ? stV + ((p - 1) % 3) * kVc : nullptr, a.spin);
             if (!cta_ok(a.status, &S.flag)) return;
             signal(F);
         }
@@ -375,7 +377,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         for (int64_t p = 0; p < nt; ++p) {
             const int64_t c0 = p * kTile;
             const int w = tile_w(p);
-            if (!wait_count(F, (unsigned)(p + 1), a.status, &S.flag)) return;
+            if (!wait_count(F, (unsigned)(p + 1), a.status, &S.flag, a.spin)) return;
             const int buf = (int)(p % 3);
             {
                 const T* mt = Mg + buf * kTile * kTile;
@@ -415,10 +417,12 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
             // The staging buffers of this step were reset during tiles p-2
             // (columns) and p-1 (tile-row), each ordered before tile p's
             // first published columns: acquire those before any poll.
-            if (!wait_count(CC, (unsigned)(p * kTile + 1), a.status, &S.flag)) return;
+            if (!wait_count(CC, (unsigned)(p * kTile + 1), a.status, &S.flag, a.spin)) return;
             if (ty < kHelpRows) {
                 const int r = h * kHelpRows + ty;
-                if (r < w2) trsm_row_vals<T>(a.diag + (c1 + r) * a.ldd + c0, w, stV + (p % 3) * kVc, a.status, sL + r * kTile);
+                if (r < w2)
+                    trsm_row_vals<T>(a.diag + (c1 + r) * a.ldd + c0, w, stV + (p % 3) * kVc, a.status, sL + r * kTile,
+                                     a.spin);
             }
             // this thread's element of tile (p+1, p+1) (last written by this CTA)
             const int rr1 = h * kHelpRows + ty, cc1 = tx;
@@ -437,7 +441,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                     sp[u] = sL + e;
                     want[u] = e / kTile < w2 && e % kTile < w;
                 }
-                const bool took = stage_take<T, U>(sp, want, v, kBarrierSpin, a.status);
+                const bool took = stage_take<T, U>(sp, want, v, a.spin, a.status);
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int e = tid + u * NT;
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                 stage_put(stT + ((p + 1) & 1) * kTile * kTile + rr1 * kTile + cc1,
                           cold - dot32<T>(&S.tmp[rr1][0], &S.tmp[cc1][0], w));
             // after the bulk TRSM: column block p applied to their rows of tile-row p+2
-            if (!group_barrier(barB, G - 2, epB, a.status, &S.flag)) return;
+            if (!group_barrier(barB, G - 2, epB, a.status, &S.flag, a.spin)) return;
             if (has_next2) {
                 load_block<T>(S.s, a.diag + c2 * a.ldd + c0, a.ldd, w3, w);  // L_{p+2,p}
                 __syncthreads();
@@ -491,10 +495,10 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                 rp = a.xinv + xr * a.xld + c0;
                 if (xr >= c0) unit = (int)(xr - c0);
             }
-            if (!trsm_row_pipe<T>(rp, w, Mp, rp3, CC, (unsigned)(p * kTile), a.status, true, unit)) break;
+            if (!trsm_row_pipe<T>(rp, w, Mp, rp3, CC, (unsigned)(p * kTile), a.status, true, a.spin, unit)) break;
         }
         if (!has_next) break;
-        if (!group_barrier(barB, G - 2, epB, a.status, &S.flag)) return;
+        if (!group_barrier(barB, G - 2, epB, a.status, &S.flag, a.spin)) return;
 
         // C(p): rank-w update of the trailing panel without tile-rows p+1, p+2
         const int64_t ntd = (m - c1 + kTile - 1) / kTile;
@@ -618,7 +622,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                     if (r < now.rows && c < now.cols) now.C[(int64_t)r * now.ldc + now.cj * kTile + c] = acc[i2][j2];
                 }
         }
-        if (!group_barrier(barC, G - kW0, epC, a.status, &S.flag)) return;
+        if (!group_barrier(barC, G - kW0, epC, a.status, &S.flag, a.spin)) return;
     }
 }
 
@@ -662,6 +666,7 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
     a.row0 = info_row0;
     a.bar = bar;
     a.status = status;
+    a.spin = spin_limit();
     e = cudaMemsetAsync(bar, 0, 16 * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     void* args[] = {(void*)&a};

@@ -20,6 +20,7 @@ struct Rec {
     int kclass;
     cudaEvent_t a, b;
     double flops;
+    double issued;
 };
 
 std::atomic<long long> g_launches{0};
@@ -51,6 +52,13 @@ void recycle_locked() {
 
 }  // namespace
 
+namespace {
+constexpr long long kDefaultSpin = 1ll << 22;
+std::atomic<long long> g_spin{kDefaultSpin};
+}  // namespace
+
+long long spin_limit() { return g_spin.load(std::memory_order_relaxed); }
+
 bool capturing(cudaStream_t s) {
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
     return cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
@@ -67,13 +75,13 @@ void prof_before(cudaStream_t s, int kclass) {
     cudaEventRecord(t_start, s);
 }
 
-void prof_after(int kclass, cudaStream_t s, double flops) {
+void prof_after(int kclass, cudaStream_t s, double flops, double issued) {
     g_launches.fetch_add(1, std::memory_order_relaxed);
     if (t_start == nullptr) return;
     std::lock_guard<std::mutex> lk(g_mu);
     cudaEvent_t e = get_event();
     cudaEventRecord(e, s);
-    g_recs.push_back(Rec{kclass, t_start, e, flops});
+    g_recs.push_back(Rec{kclass, t_start, e, flops, issued});
     t_start = nullptr;
 }
 
@@ -84,6 +92,12 @@ using namespace sgb;
 extern "C" {
 
 long long sgb_launch_count(void) { return g_launches.load(); }
+
+long long sgb_debug_spin_limit(long long polls) {
+    if (polls < 0) return g_spin.load();
+    if (polls > (1ll << 40)) polls = 1ll << 40;
+    return g_spin.exchange(polls);
+}
 
 int sgb_profile_enable(int on) { return sgb_profile_enable_classes(on ? kAllClasses : 0u); }
 
@@ -111,6 +125,16 @@ int sgb_profile_read(int kclass, long long* launches, double* ms, double* flops)
     *launches = n;
     *ms = t;
     *flops = f;
+    return SGB_OK;
+}
+
+int sgb_profile_read_issued(int kclass, double* issued) {
+    if (kclass < 0 || kclass >= SGB_KCLASS_COUNT || !issued) return SGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_mu);
+    double f = 0.0;
+    for (auto& r : g_recs)
+        if (r.kclass == kclass) f += r.issued;
+    *issued = f;
     return SGB_OK;
 }
 

@@ -409,7 +409,8 @@ __device__ void factor_tile(Smem<T>& S, T* tile, int64_t ld, int nb, int zero_ri
 // With `staged` the tile's lower part comes from that 32 x 32 staging
 // buffer (ld 32) instead of `tile`, each element taken as its producer
 // stores it and reset to the sentinel; `clear` (32 x 32) is reset to the
-// sentinel; a poll that gives up sets *status = SGB_ERR_TIMEOUT.  With
+// sentinel; a poll that gives up (after `spin` rounds) sets *status =
+// SGB_ERR_TIMEOUT.  With
 // `vcols` warp 5 also hands the factor on by value, without fences: d_k to
 // vcols[1024 + k] and column k of M to vcols[32 k .. 32 k + 31] as the
 // companion finishes them; `vclear` (32 x 32 + 32) is reset first.
@@ -422,7 +423,8 @@ template <typename T>
 __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int32_t* info, int64_t row0,
                               T* mt = nullptr, T* dv = nullptr, T* rv = nullptr, unsigned* colcount = nullptr,
                               unsigned col_base = 0, T* staged = nullptr, T* clear = nullptr,
-                              int32_t* status = nullptr, T* vcols = nullptr, T* vclear = nullptr) {
+                              int32_t* status = nullptr, T* vcols = nullptr, T* vclear = nullptr,
+                              long long spin = 1ll << 22) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     constexpr int kCons = 32 * 5;  // companion + four workers
     constexpr int kPair = 64;
@@ -441,7 +443,7 @@ __device__ void factor_tile_m(Smem<T>& S, const T* tile, int64_t ld, int nb, int
             sp[u] = staged + e;
             want[u] = r < nb && c <= r;
         }
-        timed_out = !stage_take<T, U>(sp, want, sv, 1ll << 22, status);
+        timed_out = !stage_take<T, U>(sp, want, sv, spin, status);
 #pragma unroll
         for (int u = 0; u < U; ++u)
             if (want[u]) stage_clear(staged + tid + u * kTileThreads);

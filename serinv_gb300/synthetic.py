@@ -122,6 +122,23 @@ def generate(n: int, b: int, a: int, nrhs: int = 1, seed: int = 0,
                np.ascontiguousarray(B, dtype=dt))
 
 
+def batch_shapes(count: int = 256, seed: int = 0):
+    """Shapes of the uneven batch: matrix i has n ~ U{16..256}, b drawn from
+    {32, 64, 128, 256} and a from {0, 4, 16} (one ``default_rng(seed)``
+    stream, drawn n, b, a per matrix in order); the first ``count // 2`` are
+    float32, the rest float64.  Matrix i's values come from
+    ``generate(n, b, a, 4, seed=i, dtype=...)``.  Returns a list of
+    ``(n, b, a, numpy dtype)``."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(rng.integers(16, 257))
+        b = int(rng.choice([32, 64, 128, 256]))
+        a = int(rng.choice([0, 4, 16]))
+        out.append((n, b, a, np.dtype(np.float32) if i < count // 2 else np.dtype(np.float64)))
+    return out
+
+
 def flops(n: int, b: int, a: int, nrhs: int = 0) -> dict:
     """Canonical (LAPACK-convention) flop counts of the three routines.
 

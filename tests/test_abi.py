@@ -166,3 +166,33 @@ def test_error_mapping():
     with pytest.raises(NotImplementedError):
         _lib.raise_for(_lib.SGB_ERR_UNSUPPORTED, "x")
     _lib.raise_for(_lib.SGB_OK, "x")
+
+
+def test_precision_strings():
+    assert _lib.precision_code("fp64") == _lib.SGB_PREC_NATIVE
+    assert _lib.precision_code("mixed") == _lib.SGB_PREC_MIXED
+    assert _lib.precision_code("mixed:5") == _lib.SGB_PREC_MIXED | (5 << 8)
+    assert _lib.precision_code("mixed:6:7") == _lib.SGB_PREC_MIXED | (6 << 8) | (7 << 16)
+    for bad in ("mixed:2", "mixed:6:8", "mixed:6:7:7", "half"):
+        with pytest.raises(ValueError):
+            _lib.precision_code(bad)
+
+
+def test_inverse_slice_count_workspace_and_range(lib):
+    m = _desc(n=4, b=512, a=64)
+    sz6, sz67 = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(m), _lib.precision_code("mixed:6"), ctypes.byref(sz6)) == 0
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(m), _lib.precision_code("mixed:6:7"),
+                                         ctypes.byref(sz67)) == 0
+    assert sz67.value > sz6.value  # slice scratch for 7 slices
+    bad = _lib.SGB_PREC_MIXED | (6 << 8) | (9 << 16)
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(m), bad, ctypes.byref(sz6)) == _lib.SGB_ERR_ARG
+    assert lib.sgb_pobtasi_workspace_size(ctypes.byref(m), 1 << 24 | 1, ctypes.byref(sz6)) == _lib.SGB_ERR_ARG
+
+
+def test_spin_limit_hook_roundtrip(lib):
+    prev = _lib.spin_limit()
+    assert prev == 1 << 22
+    assert _lib.spin_limit(5) == prev
+    assert _lib.spin_limit(prev) == 5
+    assert _lib.spin_limit() == prev

@@ -3,7 +3,8 @@ slice products on the tensor cores) against the oracle.
 
 Stated tolerances (relative Frobenius error per stack, against the FP64
 oracle): precision="mixed" (6 slices) <= 1e-9; "mixed:5" <= 1e-7;
-"mixed:7" (FP64-class) <= 1e-11.
+"mixed:7" (FP64-class) <= 1e-11; "mixed:6:7" (7 slices for the products
+with an explicit triangular inverse) <= 1e-9.
 """
 
 import numpy as np
@@ -18,14 +19,14 @@ from _golden import rel_err
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"mixed": 1e-9, "mixed:5": 1e-7, "mixed:7": 1e-11}
+TOL = {"mixed": 1e-9, "mixed:5": 1e-7, "mixed:7": 1e-11, "mixed:6:7": 1e-9}
 
 
 def dev(x):
     return torch.from_numpy(np.ascontiguousarray(x)).cuda()
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed:5", "mixed:7"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed:5", "mixed:7", "mixed:6:7"])
 @pytest.mark.parametrize("shape", [(4, 64, 16), (3, 100, 33), (2, 512, 64), (5, 40, 0), (1, 128, 8)])
 def test_mixed_against_oracle(precision, shape):
     n, b, a = shape
@@ -66,3 +67,32 @@ def test_mixed_medium_against_fp64_gpu():
     for x, y in zip(amx, a64):
         e = float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
         assert e <= 1e-9, e
+
+
+def test_mixed_bench_block_size_against_oracle():
+    """The benchmark's block size (b=512, a=64) at n=32 against the oracle:
+    factor, selected inverse and the 16-right-hand-side solve with the mixed
+    factor, each within the stated 1e-9."""
+    m = generate(32, 512, 64, 16, seed=512)
+    ref = m.copy()
+    oracle.pobtaf(*ref.arrays())
+    Lr = [x.copy() for x in ref.arrays()]
+    xr = m.B.copy()
+    oracle.pobtas(*Lr, xr, trans="N")
+    oracle.pobtas(*Lr, xr, trans="T")
+    oracle.pobtasi(*ref.arrays())
+    d = [dev(x) for x in m.arrays()]
+    sg.pobtaf(*d, precision="mixed")
+    L = [x.clone() for x in d]
+    for name, g, r in zip(("diag", "lower", "arrow", "tip"), L, Lr):
+        e = rel_err(g.cpu().numpy(), r)
+        assert e <= TOL["mixed"], ("factor", name, e)
+    x = dev(m.B)
+    sg.pobtas(*L, x, trans="N", precision="mixed")
+    sg.pobtas(*L, x, trans="T", precision="mixed")
+    e = rel_err(x.cpu().numpy(), xr)
+    assert e <= TOL["mixed"], ("solution", e)
+    sg.pobtasi(*d, precision="mixed")
+    for name, g, r in zip(("diag", "lower", "arrow", "tip"), d, ref.arrays()):
+        e = rel_err(g.cpu().numpy(), r)
+        assert e <= TOL["mixed"], ("selected inverse", name, e)

@@ -85,3 +85,37 @@ def test_noalloc_reports_not_spd():
 def test_noalloc_rejects_bad_descriptor():
     lib = _lib.load()
     assert lib.sgb_pobtaf_noalloc(None, 1, None, None) == _lib.SGB_ERR_ARG
+
+
+def test_noalloc_reports_timeout_in_info():
+    """A bounded device wait that gives up (poll limit 0, a test hook) is
+    reported in the caller's info word as -SGB_ERR_TIMEOUT, since the status
+    word sits in the private array; with the default limit the next call on
+    the same array is clean and exact."""
+    lib = _lib.load()
+    mat = generate(3, 100, 12, 0, seed=29)
+    A0 = [torch.from_numpy(x).cuda() for x in mat.arrays()]
+    stream = torch.cuda.current_stream().cuda_stream
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    got = [x.clone() for x in A0]
+    torch.cuda.synchronize()
+    prev = _lib.spin_limit(0)
+    try:
+        assert lib.sgb_pobtaf_noalloc(ctypes.byref(_desc(got)), 1, info.data_ptr(), stream) == 0
+        torch.cuda.synchronize()
+    finally:
+        _lib.spin_limit(prev)
+    assert int(info.item()) == -_lib.SGB_ERR_TIMEOUT
+
+    ref = [x.clone() for x in A0]
+    mref = _desc(ref)
+    need = ctypes.c_size_t(0)
+    assert lib.sgb_pobtaf_workspace_size(ctypes.byref(mref), 0, ctypes.byref(need)) == 0
+    ws = torch.empty(need.value, dtype=torch.uint8, device="cuda")
+    assert lib.sgb_pobtaf(ctypes.byref(mref), 1, 0, ws.data_ptr(), need.value, None, stream) == 0
+    got = [x.clone() for x in A0]
+    assert lib.sgb_pobtaf_noalloc(ctypes.byref(_desc(got)), 1, info.data_ptr(), stream) == 0
+    torch.cuda.synchronize()
+    assert int(info.item()) == 0
+    for x, y in zip(got, ref):
+        assert _rel(x, y) <= TOL
