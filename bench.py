@@ -570,7 +570,7 @@ def bench_kappa(args):
 
     import serinv_gb300 as sg
     from serinv_gb300 import _lib
-    from serinv_gb300.conditioning import bta_matvec, kappa_of, lanczos_extremes, shift_for_kappa
+    from bench_conditioning import bta_matvec, kappa_of, lanczos_extremes, shift_for_kappa
     from serinv_gb300.synthetic import generate_torch
 
     torch.cuda.set_device(0)

@@ -1,4 +1,6 @@
-"""Conditioning control for BTA test matrices (the kappa sweep).
+"""Conditioning control for BTA test matrices (the kappa sweep of bench.py).
+
+Measurement tooling beside the benchmark, not part of the library package.
 
 ``bta_matvec`` applies the symmetric BTA matrix given by its lower stacks;
 ``lanczos_extremes`` estimates the extreme eigenvalues of a symmetric

@@ -72,11 +72,13 @@ extern "C" {
  * error ~2^-(7S+1) of the row maxima; measured on pobtaf+pobtasi at
  * n=512, b=512, a=64: S=5 ~4e-9, S=6 ~3e-11, S=7 ~3e-13 relative.
  * FP64 storage only.
+ * With S = 7 pobtaf's TRSMs stay FP64 substitutions (the accuracy mode).
  * Bits 16-23 (3..7; 0 = S) set a separate slice count Si for the products
  * with an explicit triangular inverse -- pobtaf's rows-below-the-diagonal
  * times L_ii^{-T}, pobtasi's batched inversions and its products with
- * L_ii^{-1} -- whose error grows with the condition of L_ii:
- * SGB_PREC_MIXED | (S << 8) | (Si << 16).
+ * L_ii^{-1}: SGB_PREC_MIXED | (S << 8) | (Si << 16).  Any explicit Si takes
+ * the inverse-based TRSMs, so S = Si = 7 is 7 slices everywhere at nearly
+ * the 6-slice speed.
  * The first 4 bytes of the workspace receive a device status word (0, or
  * SGB_ERR_TIMEOUT if a bounded tensor-core wait gave up).                 */
 #define SGB_PREC_MIXED  1
@@ -167,6 +169,27 @@ int sgb_pobtaf_host(const sgb_bta* host, const sgb_bta* dev, int factorize_last_
                     void* workspace, size_t workspace_bytes, int32_t* info, void* stream);
 int sgb_pobtasi_host(const sgb_bta* host, const sgb_bta* dev, int invert_last_block, int precision,
                      void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Host-resident stacks of any size (the reference's device_streaming mode
+ * for matrices that do not fit in device memory, pobtaf.py:284-524,
+ * pobtasi.py:247-496): `host` describes the caller's host arrays (pinned for
+ * overlap).  Only `ring` blocks (D, Lo and Ar of a block per slot) and the
+ * tip are on the device at any time: blocks are uploaded on a copy stream
+ * ahead of the sweep as slots free up and downloaded once the sweep has read
+ * them for the last time, so device memory use does not grow with n.
+ * ring <= 0 selects the default (4 for pobtaf, 32 for pobtasi); pobtaf needs
+ * ring >= 2, pobtasi an even ring >= 2 (it sweeps chunks of ring/2 blocks).
+ * The workspace (size from the matching query, same ring) holds the sweep's
+ * scratch, the ring and the tip.  Same results as sgb_pobtaf / sgb_pobtasi
+ * on device stacks.  Real dtypes (complex: SGB_ERR_UNSUPPORTED).
+ */
+int sgb_pobtaf_stream_workspace_size(const sgb_bta* host, int precision, int64_t ring, size_t* bytes);
+int sgb_pobtaf_stream(const sgb_bta* host, int factorize_last_block, int precision, int64_t ring,
+                      void* workspace, size_t workspace_bytes, int32_t* info, void* stream);
+int sgb_pobtasi_stream_workspace_size(const sgb_bta* host, int precision, int64_t ring, size_t* bytes);
+int sgb_pobtasi_stream(const sgb_bta* host, int invert_last_block, int precision, int64_t ring,
+                       void* workspace, size_t workspace_bytes, void* stream);
 
 /*
  * Permuted (middle-partition) forms: the `buffer=` keyword of the reference

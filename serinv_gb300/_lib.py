@@ -92,6 +92,14 @@ _SIGNATURES = {
                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
     "sgb_pobtasi_host": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "sgb_pobtaf_stream_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_int64,
+                                                        ctypes.POINTER(ctypes.c_size_t)]),
+    "sgb_pobtaf_stream": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_int, ctypes.c_int64,
+                                         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
+    "sgb_pobtasi_stream_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_int64,
+                                                         ctypes.POINTER(ctypes.c_size_t)]),
+    "sgb_pobtasi_stream": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int, ctypes.c_int, ctypes.c_int64,
+                                          ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "sgb_pobtaf_permuted": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
     "sgb_pobtaf_permuted_workspace_size": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_int,

@@ -18,18 +18,25 @@ exporting ``__dlpack__`` (CuPy).  Device arrays are used in place on the
 current torch stream; host arrays are copied to the GPU, processed, and
 copied back in place.  Pinned host stacks (pobtaf, pobtasi) stream: the
 blocks travel up in sweep order and back as soon as they are final,
-overlapped with the computation -- the reference's ``device_streaming``
-mode, taken whenever the host memory allows it (the keyword itself is
-accepted).  All arithmetic runs in ``libserinv_gb300.so``; if it cannot be
-loaded or no GPU is present, the call raises — there is no CPU fallback.
+overlapped with the computation, with a device copy of the whole matrix as
+the working set.  ``device_streaming=True`` on host arrays (the reference's
+streaming mode) instead keeps only a ring of blocks on the device, so the
+matrix may exceed device memory; on device arrays it raises
+NotImplementedError, as the reference does.  All arithmetic runs in
+``libserinv_gb300.so``; if it cannot be loaded or no GPU is present, the
+call raises — there is no CPU fallback.
 
 Extensions (keyword-only, absent from the reference): ``precision`` —
 ``"fp64"`` (default, arithmetic in the storage type), ``"mixed"`` (FP64
 storage, block products as exact bf16 slice products on the tensor cores,
-6 slices) or ``"mixed:S"`` (S slices, 3..7; S=7 is FP64-accurate);
-``check_spd`` (pobtaf, default True) — synchronise and raise
-``numpy.linalg.LinAlgError`` on a non-positive pivot, like SciPy's
-``cholesky`` in the reference.
+6 slices), ``"mixed:S"`` (S slices, 3..7; S=7 is FP64-accurate) or
+``"mixed:S:Si"`` (Si slices for the products with an explicit triangular
+inverse, whose error grows with the conditioning); ``check_spd`` (pobtaf,
+default True) — synchronise and raise ``numpy.linalg.LinAlgError`` on a
+non-positive pivot, like SciPy's ``cholesky`` in the reference, and raise
+on a device wait that timed out (with False neither is checked and the call
+does not synchronise); ``ring_blocks`` (with ``device_streaming``) — blocks
+held on the device (default 4 for pobtaf, 32 for pobtasi).
 """
 
 from __future__ import annotations
@@ -43,7 +50,8 @@ from . import _lib
 
 _POBTAF_KW = {"device_streaming", "buffer", "factorize_last_block"}   # pobtaf.py:50
 _POBTASI_KW = {"device_streaming", "buffer", "invert_last_block"}     # pobtasi.py:45
-_EXTENSION_KW = {"precision", "check_spd"}
+_EXTENSION_KW = {"precision", "check_spd", "ring_blocks"}
+_STREAM_HOST_ONLY = "Host<->Device streaming only works when host-arrays are given."  # pobtaf.py:293-296
 
 
 # --------------------------------------------------------------------------
@@ -170,6 +178,14 @@ def _check_status(ws: torch.Tensor, precision: int, what: str, always: bool = Fa
     _lib.raise_for(code, what)
 
 
+def _copy_back(t: torch.Tensor, x) -> None:
+    """Write a contiguous host copy back into the caller's array or tensor."""
+    if isinstance(x, np.ndarray):
+        np.copyto(x, t.numpy(), casting="no")
+    else:
+        x.copy_(t)
+
+
 def _stream(device) -> int:
     return torch.cuda.current_stream(device).cuda_stream
 
@@ -211,6 +227,55 @@ def _pinned_host_stacks(arrays):
     return out
 
 
+def _streamed_host_stacks(arrays):
+    """The stacks as C-contiguous real host tensors for the streamed ring
+    (sharing the caller's memory where the layout allows, else copies to
+    write back), or raise like the reference when any is a device array.
+    Returns (tensors, writebacks) or None for complex stacks."""
+    out, back = [], []
+    for x in arrays:
+        if isinstance(x, np.ndarray):
+            if not x.flags.writeable:
+                raise ValueError("the stacks are read-only; the computation is in place")
+            t = torch.from_numpy(x) if x.flags.c_contiguous else torch.from_numpy(np.ascontiguousarray(x))
+            if not x.flags.c_contiguous:
+                back.append((t, x))
+        elif isinstance(x, torch.Tensor) and not x.is_cuda:
+            t = x.resolve_conj().resolve_neg()
+            if not t.is_contiguous() or t is not x:
+                t = t.contiguous()
+                back.append((t, x))
+        else:
+            raise NotImplementedError(_STREAM_HOST_ONLY)
+        out.append(t)
+    if len({t.dtype for t in out}) != 1:
+        raise TypeError(f"all blocks must share one dtype, got {sorted(str(t.dtype) for t in out)}")
+    if out[0].dtype not in (torch.float64, torch.float32):
+        return None
+    return out, back
+
+
+def _stream_call(entry, size_query, host, what, precision, flag, ring, with_info):
+    """Streamed ring over host stacks (the C entry `entry`): only `ring`
+    blocks and the tip are on the device; returns once the host arrays hold
+    the result."""
+    lib = _lib.load()
+    device = torch.device("cuda", torch.cuda.current_device())
+    mh = _bta_struct(*host)
+    with torch.cuda.device(device):
+        nbytes = ctypes.c_size_t(0)
+        _lib.raise_for(size_query(ctypes.byref(mh), precision, int(ring), ctypes.byref(nbytes)), what)
+        ws = _workspace(nbytes.value, device)
+        args = [ctypes.byref(mh), int(flag), precision, int(ring), ws.data_ptr(), nbytes.value]
+        info = torch.zeros(1, dtype=torch.int32, device=device) if with_info else None
+        if with_info:
+            args.append(info.data_ptr())
+        args.append(_stream(device))
+        _lib.raise_for(entry(*args), what)
+        torch.cuda.current_stream(device).synchronize()
+    return ws, info
+
+
 def _host_call(entry, size_query, host, what, precision, flag, with_info):
     """Pinned host stacks: a device copy of the same shape is the working
     set, blocks travel up and back overlapped with the sweep (the C entry
@@ -242,7 +307,9 @@ def pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_a
     """Cholesky factorization of a block tridiagonal with arrowhead SPD matrix, in place.
 
     Mirrors src/serinv/algs/pobtaf.py:11-94.  Keyword arguments:
-    ``device_streaming`` (accepted; the matrix is processed in HBM),
+    ``device_streaming`` (host arrays stream through a ring of device
+    blocks, pobtaf.py:284-524, so matrices larger than device memory work;
+    device arrays raise NotImplementedError, pobtaf.py:293-296),
     ``buffer`` (an (n, b, b) array: the permuted middle-partition
     elimination of pobtaf.py:186-281, storage precision only),
     ``factorize_last_block`` (default True).  Unknown keywords raise
@@ -260,6 +327,21 @@ def pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_a
 
     arrays = (A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_arrow_tip_block)
     _device_of(arrays)  # no GPU: fail loudly before touching the arrays
+    if kwargs.get("device_streaming", False):
+        st = _streamed_host_stacks(arrays)
+        if st is not None:
+            lib = _lib.load()
+            hs, back = st
+            ws, info = _stream_call(lib.sgb_pobtaf_stream, lib.sgb_pobtaf_stream_workspace_size, hs, "pobtaf",
+                                    precision, factorize_last_block, kwargs.get("ring_blocks", 0), True)
+            for t, x in back:
+                _copy_back(t, x)
+            _check_status(ws, precision, "pobtaf", always=check)
+            if check:
+                k = int(info.item())
+                if k > 0:
+                    raise np.linalg.LinAlgError(f"{k}-th leading minor of the array is not positive definite")
+            return
     host = _pinned_host_stacks(arrays)
     if host is not None:
         lib = _lib.load()
@@ -298,7 +380,9 @@ def pobtasi(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_
     """Selected inversion of a block tridiagonal with arrowhead matrix from its Cholesky factor, in place.
 
     Mirrors src/serinv/algs/pobtasi.py:10-89.  Keyword arguments:
-    ``device_streaming`` (accepted), ``buffer`` (the permuted variant of
+    ``device_streaming`` (host arrays stream through a ring of device blocks,
+    pobtasi.py:247-496; device arrays raise NotImplementedError), ``buffer``
+    (the permuted variant of
     pobtasi.py:175-244, storage precision only), ``invert_last_block``
     (default True).  Unknown keywords raise TypeError (pobtasi.py:45-48).
     """
@@ -313,6 +397,17 @@ def pobtasi(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_
 
     arrays = (L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_arrow_tip_block)
     _device_of(arrays)
+    if kwargs.get("device_streaming", False):
+        st = _streamed_host_stacks(arrays)
+        if st is not None:
+            lib = _lib.load()
+            hs, back = st
+            ws, _ = _stream_call(lib.sgb_pobtasi_stream, lib.sgb_pobtasi_stream_workspace_size, hs, "pobtasi",
+                                 precision, invert_last_block, kwargs.get("ring_blocks", 0), False)
+            for t, x in back:
+                _copy_back(t, x)
+            _check_status(ws, precision, "pobtasi")
+            return
     host = _pinned_host_stacks(arrays)
     if host is not None:
         lib = _lib.load()

@@ -66,13 +66,13 @@ int parse_precision(int precision, int dtype) {
 // Slice count of the products with an explicit triangular inverse (the
 // rows below a diagonal block times L_ii^{-T} in pobtaf; the batched
 // inversions and the G, H, P products of pobtasi): bits 16-23 of the
-// precision argument, 0 = the same as S.  Their error grows with the
-// condition of L_ii, so a larger count there buys accuracy at ill
-// conditioning for a small share of the time.
+// precision argument; 0 (returned as 0) = the same as S, except that S = 7
+// then keeps pobtaf's TRSMs as FP64 substitutions.  An explicit count always
+// takes the inverse-based products, so S = Si = 7 is the fast form with
+// every product at 7 slices.
 int parse_inv_slices(int precision, int S) {
     if (S <= 0) return 0;
-    const int Si = (precision >> 16) & 0xff;
-    return Si == 0 ? S : Si;
+    return (precision >> 16) & 0xff;
 }
 
 // Everything a block sweep needs besides the matrix: precision and the
@@ -214,9 +214,11 @@ template <typename T>
 struct PobtasiWs {
     size_t status, linv, linv_tip, trtri, gh, tc, tc_bytes, total;
     int64_t chunk;
-    PobtasiWs(const sgb_bta* m, int S = 0, int Si = 0) {
+    // chunk_cap: blocks per chunk at most (a streaming ring holds two chunks)
+    PobtasiWs(const sgb_bta* m, int S = 0, int Si = 0, int64_t chunk_cap = kSiChunk) {
         const int64_t n = m->n, b = m->b, a = m->a;
-        chunk = n < kSiChunk ? (n > 0 ? n : 1) : kSiChunk;
+        const int64_t cap = chunk_cap < 1 ? 1 : (chunk_cap < kSiChunk ? chunk_cap : kSiChunk);
+        chunk = n < cap ? (n > 0 ? n : 1) : cap;
         Carve c;
         status = c.take(256);
         tc_bytes = 0;
@@ -302,6 +304,45 @@ GemmProb<T> copy_prob(T* dst, int64_t ldd, const T* src, int64_t lds, int64_t M,
     return p;
 }
 
+// ---- block addresses -------------------------------------------------------
+// Block i's diagonal, lower and arrow blocks: in the stacks themselves, or in
+// a device ring of R slots (host-resident stacks streamed through HBM), slot
+// (i - off) mod R.  Batched operations over blocks lo..hi-1 need them in
+// consecutive slots (contiguous()).
+template <typename T>
+struct Blocks {
+    T* D = nullptr;
+    T* Lo = nullptr;
+    T* Ar = nullptr;
+    int64_t bb = 0, ab = 0;
+    int64_t R = 0, off = 0;
+    int64_t slot(int64_t i) const {
+        if (R == 0) return i;
+        const int64_t r = (i - off) % R;
+        return r < 0 ? r + R : r;
+    }
+    T* d(int64_t i) const { return D + slot(i) * bb; }
+    T* lo(int64_t i) const { return Lo + slot(i) * bb; }
+    T* ar(int64_t i) const { return Ar + slot(i) * ab; }
+    bool contiguous(int64_t lo_, int64_t hi) const {
+        return R == 0 || hi <= lo_ || (hi - lo_ <= R && slot(hi - 1) - slot(lo_) == hi - 1 - lo_);
+    }
+};
+
+// How a sweep's blocks reach the device when the caller's stacks are in host
+// memory.  The sweep calls need(i) before it reads block i, give(i) once
+// block i holds its final values, release(i) once it will not read block i
+// again, give_tip() once the tip is final, and finish() at the end.
+struct Link {
+    virtual ~Link() = default;
+    virtual cudaError_t start(cudaStream_t s) = 0;
+    virtual cudaError_t need(int64_t i, cudaStream_t s) = 0;
+    virtual cudaError_t give(int64_t i, cudaStream_t s) = 0;
+    virtual cudaError_t release(int64_t i, cudaStream_t s) = 0;
+    virtual cudaError_t give_tip() = 0;
+    virtual cudaError_t finish(cudaStream_t s) = 0;
+};
+
 // ---- host-resident stacks --------------------------------------------------
 // The stacks live in host memory (pinned for overlap) and are staged in a
 // device copy of the same shape.  Uploads of every block are enqueued up
@@ -313,7 +354,7 @@ GemmProb<T> copy_prob(T* dst, int64_t ldd, const T* src, int64_t lds, int64_t M,
 // costs little more than the device-resident one.
 constexpr int64_t kLinkGroup = 8;
 
-struct HostLink {
+struct HostLink : Link {
     const sgb_bta* h = nullptr;  // host stacks
     const sgb_bta* d = nullptr;  // device stacks (same shape)
     bool ascending = true;       // sweep order: pobtaf ascending, pobtasi descending
@@ -354,7 +395,7 @@ struct HostLink {
     int64_t pos(int64_t i) const { return ascending ? i : h->n - 1 - i; }
 
     // Enqueue every upload (the tip first) after the work already on s.
-    cudaError_t start(cudaStream_t s) {
+    cudaError_t start(cudaStream_t s) override {
         cudaError_t r = cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking);
         if (r == cudaSuccess) r = cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking);
         cudaEvent_t e0;
@@ -375,7 +416,7 @@ struct HostLink {
         return r;
     }
     // Block i (and every block before it in sweep order, and the tip) resident.
-    cudaError_t need(int64_t i, cudaStream_t s) {
+    cudaError_t need(int64_t i, cudaStream_t s) override {
         const int64_t g = pos(i) / kLinkGroup;
         if (g <= waited) return cudaSuccess;
         waited = g;
@@ -395,16 +436,18 @@ struct HostLink {
         return r;
     }
     // Block i is final once the launches enqueued so far on s have run.
-    cudaError_t give(int64_t i, cudaStream_t s) {
+    cudaError_t give(int64_t i, cudaStream_t s) override {
         pending.push_back(i);
         return (int64_t)pending.size() >= kLinkGroup ? flush(s) : cudaSuccess;
     }
-    cudaError_t give_tip() {
+    // the whole matrix is resident: nothing to free
+    cudaError_t release(int64_t, cudaStream_t) override { return cudaSuccess; }
+    cudaError_t give_tip() override {
         tip_pending = true;
         return cudaSuccess;
     }
     // The remaining downloads, then s waits for them.
-    cudaError_t finish(cudaStream_t s) {
+    cudaError_t finish(cudaStream_t s) override {
         cudaError_t r = flush(s);
         cudaEvent_t e;
         if (r == cudaSuccess) r = event(&e);
@@ -412,8 +455,142 @@ struct HostLink {
         if (r == cudaSuccess) r = cudaStreamWaitEvent(s, e, 0);
         return r;
     }
-    ~HostLink() {
+    ~HostLink() override {
         // released once their pending work completes
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+        if (up) cudaStreamDestroy(up);
+        if (down) cudaStreamDestroy(down);
+    }
+};
+
+// Host-resident stacks streamed through a ring of R device slots, for
+// matrices of any size (the reference's device_streaming, pobtaf.py:284-524,
+// pobtasi.py:247-496, double-buffers two blocks; here R slots).  Block i
+// lives in slot (i - off) mod R while the sweep needs it.  In sweep order
+// (ascending for pobtaf, descending for pobtasi) block q's slot was last
+// held by the block R positions earlier: its upload (copy stream `up`)
+// waits until that block was released by the sweep and downloaded (copy
+// stream `down`); uploads run ahead of the sweep as far as slots allow.
+// The tip stays on the device for the whole call.
+struct HostRing : Link {
+    const sgb_bta* h = nullptr;  // host stacks
+    char* dD = nullptr;          // ring slots: D, Lo, Ar of R blocks
+    char* dLo = nullptr;
+    char* dAr = nullptr;
+    char* dT = nullptr;          // device tip
+    int64_t R = 0, off = 0;
+    bool ascending = true;
+    size_t es = 8;
+    cudaStream_t up = nullptr, down = nullptr;
+    std::vector<cudaEvent_t> up_ev, freed, events;
+    std::vector<char> released;
+    int64_t next_up = 0;
+    bool tip_final = false;
+
+    int64_t blk(int64_t q) const { return ascending ? q : h->n - 1 - q; }
+    int64_t pos(int64_t i) const { return ascending ? i : h->n - 1 - i; }
+    int64_t slot(int64_t i) const {
+        const int64_t r = (i - off) % R;
+        return r < 0 ? r + R : r;
+    }
+    cudaError_t event(cudaEvent_t* e) {
+        cudaError_t r = cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+        if (r == cudaSuccess) events.push_back(*e);
+        return r;
+    }
+    cudaError_t copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
+        return bytes ? cudaMemcpyAsync(dst, src, bytes, kind, st) : cudaSuccess;
+    }
+    cudaError_t move(int64_t i, bool to_dev, cudaStream_t st) {
+        const int64_t n = h->n, b = h->b, a = h->a, sl = slot(i);
+        const cudaMemcpyKind k = to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+        auto mv = [&](void* hb, char* db, int64_t hoff, int64_t doff, int64_t cnt) {
+            char* hp = (char*)hb + es * hoff;
+            char* dp = db + es * doff;
+            return to_dev ? copy(dp, hp, es * cnt, k, st) : copy(hp, dp, es * cnt, k, st);
+        };
+        cudaError_t r = mv(h->diag, dD, i * b * b, sl * b * b, b * b);
+        if (r == cudaSuccess && i < n - 1) r = mv(h->lower, dLo, i * b * b, sl * b * b, b * b);
+        if (r == cudaSuccess && a) r = mv(h->arrow, dAr, i * a * b, sl * a * b, a * b);
+        return r;
+    }
+    // Enqueue the uploads whose slots are free, in sweep order.
+    cudaError_t pump() {
+        const int64_t n = h->n;
+        while (next_up < n) {
+            const int64_t q = next_up;
+            if (q >= R && !released[(size_t)(q - R)]) break;
+            const int64_t i = blk(q), sl = slot(i);
+            cudaError_t r = cudaSuccess;
+            if (q >= R) r = cudaStreamWaitEvent(up, freed[(size_t)sl], 0);
+            if (r == cudaSuccess) r = move(i, true, up);
+            if (r == cudaSuccess) r = cudaEventRecord(up_ev[(size_t)sl], up);
+            if (r != cudaSuccess) return r;
+            ++next_up;
+        }
+        return cudaSuccess;
+    }
+    cudaError_t start(cudaStream_t s) override {
+        const int64_t n = h->n, a = h->a;
+        released.assign((size_t)n, 0);
+        up_ev.resize((size_t)R);
+        freed.resize((size_t)R);
+        cudaError_t r = cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking);
+        if (r == cudaSuccess) r = cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking);
+        for (int64_t k = 0; k < R && r == cudaSuccess; ++k) {
+            r = event(&up_ev[(size_t)k]);
+            if (r == cudaSuccess) r = event(&freed[(size_t)k]);
+        }
+        cudaEvent_t e0, et;
+        if (r == cudaSuccess) r = event(&e0);
+        if (r == cudaSuccess) r = cudaEventRecord(e0, s);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(up, e0, 0);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(down, e0, 0);
+        if (r == cudaSuccess && a) r = copy(dT, h->tip, es * a * a, cudaMemcpyHostToDevice, up);
+        if (r == cudaSuccess) r = event(&et);
+        if (r == cudaSuccess) r = cudaEventRecord(et, up);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(s, et, 0);
+        if (r == cudaSuccess) r = pump();
+        return r;
+    }
+    cudaError_t need(int64_t i, cudaStream_t s) override {
+        const int64_t q = pos(i);
+        cudaError_t r = pump();
+        if (r != cudaSuccess) return r;
+        if (next_up <= q) return cudaErrorInvalidValue;  // ring too small for the sweep
+        return cudaStreamWaitEvent(s, up_ev[(size_t)slot(i)], 0);
+    }
+    // final values leave when the slot is released
+    cudaError_t give(int64_t, cudaStream_t) override { return cudaSuccess; }
+    cudaError_t release(int64_t i, cudaStream_t s) override {
+        const int64_t q = pos(i);
+        if (released[(size_t)q]) return cudaSuccess;
+        cudaEvent_t e;
+        cudaError_t r = event(&e);
+        if (r == cudaSuccess) r = cudaEventRecord(e, s);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(down, e, 0);
+        if (r == cudaSuccess) r = move(i, false, down);
+        if (r == cudaSuccess) r = cudaEventRecord(freed[(size_t)slot(i)], down);
+        if (r != cudaSuccess) return r;
+        released[(size_t)q] = 1;
+        return pump();
+    }
+    cudaError_t give_tip() override {
+        tip_final = true;
+        return cudaSuccess;
+    }
+    cudaError_t finish(cudaStream_t s) override {
+        cudaEvent_t e, d;
+        cudaError_t r = event(&e);
+        if (r == cudaSuccess) r = cudaEventRecord(e, s);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(down, e, 0);
+        if (r == cudaSuccess && h->a) r = copy(h->tip, dT, es * h->a * h->a, cudaMemcpyDeviceToHost, down);
+        if (r == cudaSuccess) r = event(&d);
+        if (r == cudaSuccess) r = cudaEventRecord(d, down);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(s, d, 0);
+        return r;
+    }
+    ~HostRing() override {
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (up) cudaStreamDestroy(up);
         if (down) cudaStreamDestroy(down);
@@ -426,12 +603,16 @@ struct HostLink {
 //   D_{i+1} -= Lo_i Lo_i^T, Ar_{i+1} -= Ar_i Lo_i^T, T -= Ar_i Ar_i^T  (:143-159)
 template <typename T>
 int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* ws, int32_t* info, cudaStream_t s,
-               HostLink* hl = nullptr, T* xall = nullptr, bool* xall_filled = nullptr) {
+               Link* hl = nullptr, T* xall = nullptr, bool* xall_filled = nullptr, int64_t ring = 0) {
     const int64_t n = m->n, b = m->b, a = m->a;
-    T* D = (T*)m->diag;
-    T* Lo = (T*)m->lower;
-    T* Ar = (T*)m->arrow;
     T* Tp = (T*)m->tip;
+    Blocks<T> B;
+    B.D = (T*)m->diag;
+    B.Lo = (T*)m->lower;
+    B.Ar = (T*)m->arrow;
+    B.bb = b * b;
+    B.ab = a * b;
+    B.R = ring;
     PobtafWs<T> L(m, S, Si);
     T* tinv = (T*)((char*)ws + L.tinv);
     Ctx cx;
@@ -440,7 +621,7 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* 
     cx.tc_bytes = L.tc_bytes;
     cx.status = (int32_t*)((char*)ws + L.status);
     Ctx cxi = cx;  // products with L_ii^{-T}
-    cxi.slices = Si;
+    cxi.slices = Si ? Si : S;
     const int64_t bb = b * b, ab = a * b;
     T* Xinv0 = (T*)((char*)ws + L.xinv);
 
@@ -462,12 +643,12 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* 
     const bool persistent = (!captured || pgrid > 0) && b > 2 * kTile;
     // 7 slices is the accuracy mode: its TRSMs stay FP64 substitutions (the
     // product with L_ii^{-T} carries kappa(L_ii) times the slice truncation)
-    bool mixed_inverse = S != 0 && S < 7 && persistent;
+    bool mixed_inverse = S != 0 && (S < 7 || Si != 0) && persistent;
     // the launch writes only the upper block triangle of L_ii^{-T}
     // xall (n b x b blocks): keep every L_ii^{-T} for later sweeps on this factor
     if (mixed_inverse) SGB_TRY(cudaMemsetAsync(xall ? xall : Xinv0, 0, sizeof(T) * bb * (xall ? n : 1), s));
     auto factor = [&](int64_t i, RowSet<T> r1, RowSet<T> r2) -> int {
-        T* Di = D + i * bb;
+        T* Di = B.d(i);
         T* Xinv = xall ? xall + i * bb : Xinv0;
         if (mixed_inverse) {
             RowSet<T> none{nullptr, 0, b};
@@ -501,9 +682,9 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* 
 
     if (hl) SGB_TRY(hl->start(s));
     for (int64_t i = 0; i < n - 1; ++i) {
-        RowSet<T> r1{Lo + i * bb, b, b};
-        RowSet<T> r2{a ? Ar + i * ab : nullptr, a, b};
         if (hl) SGB_TRY(hl->need(i, s));
+        RowSet<T> r1{B.lo(i), b, b};
+        RowSet<T> r2{a ? B.ar(i) : nullptr, a, b};
         int rc = factor(i, r1, r2);
         if (rc != SGB_OK) return rc;
         if (hl) SGB_TRY(hl->give(i, s));
@@ -515,10 +696,10 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* 
         {   // D_{i+1} -= Lo_i Lo_i^T
             GemmProb<T> p = prob<T>();
             p.M = p.N = (int32_t)b;
-            set_term<T>(p, 0, Lo + i * bb, b, 0, Lo + i * bb, b, 1, b);
+            set_term<T>(p, 0, B.lo(i), b, 0, B.lo(i), b, 1, b);
             p.alpha = T(-1);
             p.beta = T(1);
-            p.Cin = p.Cout = D + (i + 1) * bb;
+            p.Cin = p.Cout = B.d(i + 1);
             p.ldcin = p.ldc = b;
             p.lower_only = next_factored ? 1 : 0;
             pr[np++] = p;
@@ -527,15 +708,15 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* 
             GemmProb<T> p = prob<T>();  // Ar_{i+1} -= Ar_i Lo_i^T
             p.M = (int32_t)a;
             p.N = (int32_t)b;
-            set_term<T>(p, 0, Ar + i * ab, b, 0, Lo + i * bb, b, 1, b);
+            set_term<T>(p, 0, B.ar(i), b, 0, B.lo(i), b, 1, b);
             p.alpha = T(-1);
             p.beta = T(1);
-            p.Cin = p.Cout = Ar + (i + 1) * ab;
+            p.Cin = p.Cout = B.ar(i + 1);
             p.ldcin = p.ldc = b;
             pr[np++] = p;
             GemmProb<T> q = prob<T>();  // T -= Ar_i Ar_i^T
             q.M = q.N = (int32_t)a;
-            set_term<T>(q, 0, Ar + i * ab, b, 0, Ar + i * ab, b, 1, b);
+            set_term<T>(q, 0, B.ar(i), b, 0, B.ar(i), b, 1, b);
             q.alpha = T(-1);
             q.beta = T(1);
             q.Cin = q.Cout = Tp;
@@ -544,19 +725,20 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* 
             pr[np++] = q;
         }
         SGB_TRY(run_gemm<T>(cx, pr, np, s));
+        if (hl) SGB_TRY(hl->release(i, s));  // block i is not read again
     }
 
     if (hl) SGB_TRY(hl->need(n - 1, s));
     if (factorize_last_block) {
         const int64_t i = n - 1;
         RowSet<T> r1{nullptr, 0, b};
-        RowSet<T> r2{a ? Ar + i * ab : nullptr, a, b};
+        RowSet<T> r2{a ? B.ar(i) : nullptr, a, b};
         int rc = factor(i, r1, r2);
         if (rc != SGB_OK) return rc;
         if (a) {
             GemmProb<T> q = prob<T>();  // T -= Ar_{n-1} Ar_{n-1}^T  (:177-180)
             q.M = q.N = (int32_t)a;
-            set_term<T>(q, 0, Ar + i * ab, b, 0, Ar + i * ab, b, 1, b);
+            set_term<T>(q, 0, B.ar(i), b, 0, B.ar(i), b, 1, b);
             q.alpha = T(-1);
             q.beta = T(1);
             q.Cin = q.Cout = Tp;
@@ -570,6 +752,7 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* 
     }
     if (hl) {
         SGB_TRY(hl->give(n - 1, s));
+        SGB_TRY(hl->release(n - 1, s));
         SGB_TRY(hl->give_tip());
         SGB_TRY(hl->finish(s));
     }
@@ -597,13 +780,19 @@ int pobtaf_run(const sgb_bta* m, int factorize_last_block, int S, int Si, void* 
 // diagonal block itself and the outputs overwrite the factor in place.
 template <typename T>
 int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws, cudaStream_t s,
-                HostLink* hl = nullptr, const T* xall = nullptr) {
+                Link* hl = nullptr, const T* xall = nullptr, int64_t ring = 0) {
     const int64_t n = m->n, b = m->b, a = m->a;
-    T* D = (T*)m->diag;
-    T* Lo = (T*)m->lower;
-    T* Ar = (T*)m->arrow;
     T* Tp = (T*)m->tip;
-    PobtasiWs<T> W(m, S, Si);
+    // a ring holds two chunks: the one being swept and the one above it
+    PobtasiWs<T> W(m, S, Si, ring ? ring / 2 : kSiChunk);
+    Blocks<T> B;
+    B.D = (T*)m->diag;
+    B.Lo = (T*)m->lower;
+    B.Ar = (T*)m->arrow;
+    B.bb = b * b;
+    B.ab = a * b;
+    B.R = ring;
+    B.off = invert_last_block ? n : n - 1;  // chunks end at multiples of the chunk size from here
     char* base = (char*)ws;
     Ctx cx;
     cx.slices = S;
@@ -611,7 +800,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws
     cx.tc_bytes = W.tc_bytes;
     cx.status = (int32_t*)(base + W.status);
     Ctx cxi = cx;  // the inversions and the products with L_ii^{-1}
-    cxi.slices = Si;
+    cxi.slices = Si ? Si : S;
     T* Linv = (T*)(base + W.linv);
     T* Ltinv = (T*)(base + W.linv_tip);
     T* trs = (T*)(base + W.trtri);
@@ -640,8 +829,9 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws
     for (int64_t hi = ninv; hi > 0; hi -= W.chunk) {
         const int64_t lo = hi > W.chunk ? hi - W.chunk : 0;
         if (hl) SGB_TRY(hl->need(lo, s));
+        if (!B.contiguous(lo, hi)) return SGB_ERR_WORKSPACE;
         // with xall the inverses exist already, as L_jj^{-T}: operands are read transposed
-        if (!xall) SGB_TRY(trtri_run<T>(cxi, D + lo * bb, b, hi - lo, Linv, trs, s));
+        if (!xall) SGB_TRY(trtri_run<T>(cxi, B.d(lo), b, hi - lo, Linv, trs, s));
         for (int64_t j0 = lo; j0 < hi; j0 += tcb) {
             const int64_t jn = (hi - j0) < tcb ? (hi - j0) : tcb;
             const int64_t ng = (j0 + jn <= n - 1) ? jn : (n - 1 - j0);  // blocks with a Lo_j
@@ -654,7 +844,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws
                 GemmProb<T> p = prob<T>();
                 p.M = p.N = (int32_t)b;
                 p.batch = (int32_t)ng;
-                set_term<T>(p, 0, Lo + j0 * bb, b, 0, Lj, b, tl, b, KM_GE_N0);
+                set_term<T>(p, 0, B.lo(j0), b, 0, Lj, b, tl, b, KM_GE_N0);
                 p.term[0].strideA = bb;
                 p.term[0].strideB = bb;
                 p.Cout = GHj;
@@ -667,7 +857,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws
                 p.M = (int32_t)a;
                 p.N = (int32_t)b;
                 p.batch = (int32_t)jn;
-                set_term<T>(p, 0, Ar + j0 * ab, b, 0, Lj, b, tl, b, KM_GE_N0);
+                set_term<T>(p, 0, B.ar(j0), b, 0, Lj, b, tl, b, KM_GE_N0);
                 p.term[0].strideA = ab;
                 p.term[0].strideB = bb;
                 p.Cout = GHj + bb;
@@ -682,7 +872,7 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws
                 set_term<T>(p, 0, Lj, b, 1 - tl, Lj, b, tl, b, KM_GE_M0);
                 p.term[0].strideA = bb;
                 p.term[0].strideB = bb;
-                p.Cout = D + j0 * bb;
+                p.Cout = B.d(j0);
                 p.ldc = b;
                 p.strideC = bb;
                 pr[np++] = p;
@@ -698,10 +888,10 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws
             if (has_next) {  // X_{i+1,i} = -(X_{i+1,i+1} G_i + X_{A,i+1}^T H_i)  (:150-155)
                 GemmProb<T> p = prob<T>();
                 p.M = p.N = (int32_t)b;
-                set_term<T>(p, 0, D + (i + 1) * bb, b, 0, G, b, 0, b);
-                if (a) set_term<T>(p, 1, Ar + (i + 1) * ab, b, 1, H, b, 0, a);
+                set_term<T>(p, 0, B.d(i + 1), b, 0, G, b, 0, b);
+                if (a) set_term<T>(p, 1, B.ar(i + 1), b, 1, H, b, 0, a);
                 p.alpha = T(-1);
-                p.Cout = Lo + i * bb;
+                p.Cout = B.lo(i);
                 p.ldc = b;
                 pr[np++] = p;
             }
@@ -710,10 +900,10 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws
                 p.M = (int32_t)a;
                 p.N = (int32_t)b;
                 int t = 0;
-                if (has_next) set_term<T>(p, t++, Ar + (i + 1) * ab, b, 0, G, b, 0, b);
+                if (has_next) set_term<T>(p, t++, B.ar(i + 1), b, 0, G, b, 0, b);
                 set_term<T>(p, t, Tp, a, 0, H, b, 0, a);
                 p.alpha = T(-1);
-                p.Cout = Ar + i * ab;
+                p.Cout = B.ar(i);
                 p.ldc = b;
                 pr[np++] = p;
             }
@@ -723,21 +913,25 @@ int pobtasi_run(const sgb_bta* m, int invert_last_block, int S, int Si, void* ws
                 GemmProb<T> p = prob<T>();
                 p.M = p.N = (int32_t)b;
                 int t = 0;
-                if (has_next) set_term<T>(p, t++, Lo + i * bb, b, 1, G, b, 0, b);
-                if (a) set_term<T>(p, t++, Ar + i * ab, b, 1, H, b, 0, a);
+                if (has_next) set_term<T>(p, t++, B.lo(i), b, 1, G, b, 0, b);
+                if (a) set_term<T>(p, t++, B.ar(i), b, 1, H, b, 0, a);
                 p.alpha = T(-1);
                 p.beta = T(1);
-                p.Cin = D + i * bb;
+                p.Cin = B.d(i);
                 p.ldcin = b;
-                p.Cout = D + i * bb;
+                p.Cout = B.d(i);
                 p.ldc = b;
                 SGB_TRY(run_gemm<T>(cx, &p, 1, s));
             }
-            if (hl) SGB_TRY(hl->give(i, s));
+            if (hl) {
+                SGB_TRY(hl->give(i, s));
+                if (has_next) SGB_TRY(hl->release(i + 1, s));  // block i+1 was read for the last time
+            }
         }
     }
     if (hl) {
         if (!invert_last_block) SGB_TRY(hl->give(n - 1, s));
+        SGB_TRY(hl->release(0, s));
         SGB_TRY(hl->finish(s));
     }
     return SGB_OK;
@@ -1252,6 +1446,64 @@ int plan_item(const sgb_bta* m, int ops, int precision, void* rhs, int64_t nrhs,
 }
 
 namespace {
+
+// ---- streamed host-resident stacks ----------------------------------------
+// Workspace of sgb_pobtaf_stream / sgb_pobtasi_stream: the sweep's own
+// workspace for the matrix's shape, then the ring (R slots of D, Lo and Ar
+// blocks) and the device tip.
+constexpr int64_t kRingPobtaf = 4;
+constexpr int64_t kRingPobtasi = 32;
+
+int64_t ring_slots(int64_t ring, int64_t dflt, bool even) {
+    int64_t r = ring > 0 ? ring : dflt;
+    if (even) r -= r % 2;
+    return r;
+}
+
+struct StreamWs {
+    size_t sweep = 0, ringD = 0, ringLo = 0, ringAr = 0, tip = 0, total = 0;
+    StreamWs(const sgb_bta* m, size_t sweep_bytes, int64_t R) {
+        const size_t es = m->dtype == SGB_F64 ? 8 : 4;
+        const size_t b = (size_t)m->b, a = (size_t)m->a;
+        Carve c;
+        sweep = c.take(sweep_bytes);
+        ringD = c.take(es * (size_t)R * b * b);
+        ringLo = c.take(es * (size_t)R * b * b);
+        ringAr = c.take(es * (size_t)R * a * b);
+        tip = c.take(es * a * a);
+        total = c.off;
+    }
+};
+
+// The device-side descriptor of the ring: the sweeps address block i in
+// slot (i - off) mod R through Blocks.
+sgb_bta ring_desc(const sgb_bta* host, char* ws, const StreamWs& L) {
+    sgb_bta d = *host;
+    d.diag = ws + L.ringD;
+    d.lower = ws + L.ringLo;
+    d.arrow = ws + L.ringAr;
+    d.tip = ws + L.tip;
+    return d;
+}
+
+int stream_sizes(const sgb_bta* host, int precision, int64_t ring, bool inverse, int64_t* R, size_t* sweep,
+                 size_t* total) {
+    int rc = check_bta(host);
+    if (rc) return rc;
+    const int S = parse_precision(precision, host->dtype);
+    if (S < 0) return -S;
+    const int Si = parse_inv_slices(precision, S);
+    *R = inverse ? ring_slots(ring, kRingPobtasi, true) : ring_slots(ring, kRingPobtaf, false);
+    if (*R < 2 || *R > ((int64_t)1 << 20)) return SGB_ERR_SHAPE;
+    if (inverse)
+        *sweep = host->dtype == SGB_F64 ? PobtasiWs<double>(host, S, Si, *R / 2).total
+                                        : PobtasiWs<float>(host, S, Si, *R / 2).total;
+    else
+        *sweep = host->dtype == SGB_F64 ? PobtafWs<double>(host, S, Si).total : PobtafWs<float>(host, S, Si).total;
+    *total = StreamWs(host, *sweep, *R).total;
+    return SGB_OK;
+}
+
 }  // namespace
 }  // namespace sgb
 
@@ -1604,6 +1856,81 @@ int sgb_pobtaf_host(const sgb_bta* host, const sgb_bta* dev, int factorize_last_
     if (dev->dtype == SGB_F64)
         return pobtaf_run<double>(dev, factorize_last_block, S, Si, workspace, info, s, &hl);
     return pobtaf_run<float>(dev, factorize_last_block, S, Si, workspace, info, s, &hl);
+}
+
+int sgb_pobtaf_stream_workspace_size(const sgb_bta* host, int precision, int64_t ring, size_t* bytes) {
+    if (cx_dtype(host)) return SGB_ERR_UNSUPPORTED;
+    if (!bytes) return SGB_ERR_ARG;
+    int64_t R = 0;
+    size_t sweep = 0;
+    return stream_sizes(host, precision, ring, false, &R, &sweep, bytes);
+}
+
+int sgb_pobtasi_stream_workspace_size(const sgb_bta* host, int precision, int64_t ring, size_t* bytes) {
+    if (cx_dtype(host)) return SGB_ERR_UNSUPPORTED;
+    if (!bytes) return SGB_ERR_ARG;
+    int64_t R = 0;
+    size_t sweep = 0;
+    return stream_sizes(host, precision, ring, true, &R, &sweep, bytes);
+}
+
+int sgb_pobtaf_stream(const sgb_bta* host, int factorize_last_block, int precision, int64_t ring, void* workspace,
+                      size_t workspace_bytes, int32_t* info, void* stream) {
+    if (cx_dtype(host)) return SGB_ERR_UNSUPPORTED;
+    int64_t R = 0;
+    size_t sweep = 0, total = 0;
+    int rc = stream_sizes(host, precision, ring, false, &R, &sweep, &total);
+    if (rc) return rc;
+    if ((rc = check_ws(workspace, workspace_bytes, total))) return rc;
+    const int S = parse_precision(precision, host->dtype);
+    const int Si = parse_inv_slices(precision, S);
+    const StreamWs L(host, sweep, R);
+    const sgb_bta dm = ring_desc(host, (char*)workspace, L);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
+    SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
+    HostRing hr;
+    hr.h = host;
+    hr.dD = (char*)dm.diag;
+    hr.dLo = (char*)dm.lower;
+    hr.dAr = (char*)dm.arrow;
+    hr.dT = (char*)dm.tip;
+    hr.R = R;
+    hr.off = 0;
+    hr.ascending = true;
+    hr.es = host->dtype == SGB_F64 ? 8 : 4;
+    if (host->dtype == SGB_F64)
+        return pobtaf_run<double>(&dm, factorize_last_block, S, Si, workspace, info, s, &hr, nullptr, nullptr, R);
+    return pobtaf_run<float>(&dm, factorize_last_block, S, Si, workspace, info, s, &hr, nullptr, nullptr, R);
+}
+
+int sgb_pobtasi_stream(const sgb_bta* host, int invert_last_block, int precision, int64_t ring, void* workspace,
+                       size_t workspace_bytes, void* stream) {
+    if (cx_dtype(host)) return SGB_ERR_UNSUPPORTED;
+    int64_t R = 0;
+    size_t sweep = 0, total = 0;
+    int rc = stream_sizes(host, precision, ring, true, &R, &sweep, &total);
+    if (rc) return rc;
+    if ((rc = check_ws(workspace, workspace_bytes, total))) return rc;
+    const int S = parse_precision(precision, host->dtype);
+    const int Si = parse_inv_slices(precision, S);
+    const StreamWs L(host, sweep, R);
+    const sgb_bta dm = ring_desc(host, (char*)workspace, L);
+    cudaStream_t s = (cudaStream_t)stream;
+    SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
+    HostRing hr;
+    hr.h = host;
+    hr.dD = (char*)dm.diag;
+    hr.dLo = (char*)dm.lower;
+    hr.dAr = (char*)dm.arrow;
+    hr.dT = (char*)dm.tip;
+    hr.R = R;
+    hr.off = invert_last_block ? host->n : host->n - 1;  // the sweep's chunk alignment
+    hr.ascending = false;
+    hr.es = host->dtype == SGB_F64 ? 8 : 4;
+    if (host->dtype == SGB_F64)
+        return pobtasi_run<double>(&dm, invert_last_block, S, Si, workspace, s, &hr, nullptr, R);
+    return pobtasi_run<float>(&dm, invert_last_block, S, Si, workspace, s, &hr, nullptr, R);
 }
 
 int sgb_pobtasi_host(const sgb_bta* host, const sgb_bta* dev, int invert_last_block, int precision,

@@ -300,4 +300,6 @@ def main(ref_root: str, only: str | None = None) -> None:
 if __name__ == "__main__":
     args = [x for x in sys.argv[1:] if not x.startswith("--only=")]
     only = next((x.split("=", 1)[1] for x in sys.argv[1:] if x.startswith("--only=")), None)
-    main(args[0] if args else "/root/reference", only)
+    if len(args) != 1:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT [--only=permuted|complex]")
+    main(args[0], only)

@@ -196,3 +196,23 @@ def test_spin_limit_hook_roundtrip(lib):
     assert _lib.spin_limit(5) == prev
     assert _lib.spin_limit(prev) == 5
     assert _lib.spin_limit() == prev
+
+
+def test_stream_workspace_does_not_grow_with_n(lib):
+    """The streamed ring's device footprint depends on the ring, not on n."""
+    sizes = []
+    for n in (10, 1000, 1_000_000):
+        m = _desc(n=n, b=512, a=64)
+        for q, ring in ((lib.sgb_pobtaf_stream_workspace_size, 4), (lib.sgb_pobtasi_stream_workspace_size, 32)):
+            sz = ctypes.c_size_t(0)
+            assert q(ctypes.byref(m), 0, ring, ctypes.byref(sz)) == 0
+            sizes.append((q.__name__, sz.value))
+    by = {}
+    for name, v in sizes[2:]:  # n = 10 may be smaller (pobtasi chunk shrinks with n)
+        by.setdefault(name, set()).add(v)
+    assert all(len(v) == 1 for v in by.values()), by
+    m = _desc(n=100, b=512, a=64)
+    sz = ctypes.c_size_t(0)
+    assert lib.sgb_pobtaf_stream_workspace_size(ctypes.byref(m), 0, 1, ctypes.byref(sz)) == _lib.SGB_ERR_SHAPE
+    cm = _desc(n=100, b=64, a=8, dtype=_lib.SGB_C128)
+    assert lib.sgb_pobtaf_stream_workspace_size(ctypes.byref(cm), 0, 4, ctypes.byref(sz)) == _lib.SGB_ERR_UNSUPPORTED

@@ -4,7 +4,8 @@ slice products on the tensor cores) against the oracle.
 Stated tolerances (relative Frobenius error per stack, against the FP64
 oracle): precision="mixed" (6 slices) <= 1e-9; "mixed:5" <= 1e-7;
 "mixed:7" (FP64-class) <= 1e-11; "mixed:6:7" (7 slices for the products
-with an explicit triangular inverse) <= 1e-9.
+with an explicit triangular inverse) <= 1e-9; "mixed:7:7" (7 slices
+everywhere, TRSMs through the explicit inverse) <= 1e-11.
 """
 
 import numpy as np
@@ -19,14 +20,14 @@ from _golden import rel_err
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"mixed": 1e-9, "mixed:5": 1e-7, "mixed:7": 1e-11, "mixed:6:7": 1e-9}
+TOL = {"mixed": 1e-9, "mixed:5": 1e-7, "mixed:7": 1e-11, "mixed:6:7": 1e-9, "mixed:7:7": 1e-11}
 
 
 def dev(x):
     return torch.from_numpy(np.ascontiguousarray(x)).cuda()
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed:5", "mixed:7", "mixed:6:7"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed:5", "mixed:7", "mixed:6:7", "mixed:7:7"])
 @pytest.mark.parametrize("shape", [(4, 64, 16), (3, 100, 33), (2, 512, 64), (5, 40, 0), (1, 128, 8)])
 def test_mixed_against_oracle(precision, shape):
     n, b, a = shape
