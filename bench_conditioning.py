@@ -74,7 +74,7 @@ def shift_for_kappa(lmin0: float, lmax0: float, kappa: float) -> float:
 
 def kappa_of(D, Lo, Ar, T, steps: int = 60):
     """(kappa, lambda_min, lambda_max) of the SPD BTA matrix, measured on the GPU."""
-    from .algs import pobtaf, pobtas
+    from serinv_gb300.algs import pobtaf, pobtas
 
     n, b, a = D.shape[0], D.shape[1], Ar.shape[1]
     N = n * b + a

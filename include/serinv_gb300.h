@@ -195,8 +195,12 @@ int sgb_pobtasi_stream(const sgb_bta* host, int invert_last_block, int precision
  * Permuted (middle-partition) forms: the `buffer=` keyword of the reference
  * functions.  buffer (n, b, b) carries the fill-in between block 0 and the
  * eliminated blocks 1..n-2; blocks 0, n-1 and the tip form the reduced
- * system that the caller factorizes, inverts or solves itself.  SGB_PREC_NATIVE
- * only (SGB_ERR_UNSUPPORTED otherwise); n >= 2.
+ * system that the caller factorizes, inverts or solves itself.  n >= 2.
+ * SGB_PREC_MIXED (FP64 storage) runs pobtaf's diagonal blocks through the
+ * column-block kernel with L_ii^{-T} and every block product on the tensor
+ * cores, and pobtasi's products likewise; the solve runs in the storage
+ * precision in either mode, as sgb_pobtas does.  The first 4 bytes of the
+ * pobtaf / pobtasi workspace receive the device status word.
  *
  * sgb_pobtaf_permuted: pobtaf(..., buffer=) (src/serinv/algs/pobtaf.py:
  *   58-76, _pobtaf_permuted :186-281).  Workspace:

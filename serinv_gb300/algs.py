@@ -9,7 +9,7 @@ exception types as the reference's sequential functions:
 * ``pobtf`` / ``pobtsi`` / ``pobts`` — src/serinv/algs/pobtf.py, pobtsi.py,
   pobts.py (the same calls with an empty arrow stack)
 
-``buffer=`` selects the permuted middle-partition forms (storage precision).
+``buffer=`` selects the permuted middle-partition forms (either precision).
 float64, float32, complex128 and complex64 stacks are accepted; complex
 matrices are Hermitian and run through their real embedding.
 
@@ -311,7 +311,7 @@ def pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, A_lower_arrow_blocks, A_a
     blocks, pobtaf.py:284-524, so matrices larger than device memory work;
     device arrays raise NotImplementedError, pobtaf.py:293-296),
     ``buffer`` (an (n, b, b) array: the permuted middle-partition
-    elimination of pobtaf.py:186-281, storage precision only),
+    elimination of pobtaf.py:186-281),
     ``factorize_last_block`` (default True).  Unknown keywords raise
     TypeError (pobtaf.py:50-53).
     """
@@ -383,7 +383,7 @@ def pobtasi(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_
     ``device_streaming`` (host arrays stream through a ring of device blocks,
     pobtasi.py:247-496; device arrays raise NotImplementedError), ``buffer``
     (the permuted variant of
-    pobtasi.py:175-244, storage precision only), ``invert_last_block``
+    pobtasi.py:175-244), ``invert_last_block``
     (default True).  Unknown keywords raise TypeError (pobtasi.py:45-48).
     """
     unexpected = set(kwargs) - _POBTASI_KW - _EXTENSION_KW
@@ -441,7 +441,7 @@ def pobtas(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_a
     ``B <- L^{-1} B``, ``"T"``/``"C"`` computes ``B <- L^{-T} B``, anything
     else raises ValueError (pobtas.py:160-161).  ``partial=True`` skips the
     last diagonal block and the tip.  ``buffer`` selects the permuted solve
-    of pobtas.py:164-218 (storage precision only).  ``device_streaming``
+    of pobtas.py:164-218 (storage precision).  ``device_streaming``
     raises NotImplementedError (pobtas.py:33-36,49-52).  Like the reference,
     unknown keywords are ignored.  For arrow width 0 the call is the
     arrow-free solve of src/serinv/algs/pobts.py:57-118 (the reference's
@@ -489,13 +489,6 @@ def pobtas(L_diagonal_blocks, L_lower_diagonal_blocks, L_lower_arrow_blocks, L_a
 # permuted (middle-partition) forms: the ``buffer=`` keyword
 
 
-def _native_only(kwargs, what: str) -> int:
-    precision = _precision(kwargs)
-    if precision != _lib.SGB_PREC_NATIVE:
-        raise NotImplementedError(f"{what} with buffer= computes in the storage precision only")
-    return precision
-
-
 def _check_buffer(buf: torch.Tensor, D: torch.Tensor) -> None:
     n, b = D.shape[0], D.shape[1]
     if tuple(buf.shape) != (n, b, b):
@@ -506,7 +499,7 @@ def _check_buffer(buf: torch.Tensor, D: torch.Tensor) -> None:
 
 def _pobtaf_permuted(D, Lo, Ar, T, buffer, kwargs):
     """pobtaf(..., buffer=): src/serinv/algs/pobtaf.py:186-281."""
-    precision = _native_only(kwargs, "pobtaf")
+    precision = _precision(kwargs)
     check = bool(kwargs.get("check_spd", True))
     lib = _lib.load()
     device, w = _prepare((D, Lo, Ar, T, buffer),
@@ -524,6 +517,7 @@ def _pobtaf_permuted(D, Lo, Ar, T, buffer, kwargs):
                                      info.data_ptr(), _stream(device))
         _lib.raise_for(rc, "pobtaf")
         _finish(w)
+        _check_status(ws, precision, "pobtaf", always=check)
         if check:
             k = int(info.item())
             if k > 0:
@@ -532,7 +526,7 @@ def _pobtaf_permuted(D, Lo, Ar, T, buffer, kwargs):
 
 def _pobtasi_permuted(D, Lo, Ar, T, buffer, kwargs):
     """pobtasi(..., buffer=): src/serinv/algs/pobtasi.py:175-244."""
-    precision = _native_only(kwargs, "pobtasi")
+    precision = _precision(kwargs)
     lib = _lib.load()
     device, w = _prepare((D, Lo, Ar, T, buffer),
                          ("L_diagonal_blocks", "L_lower_diagonal_blocks", "L_lower_arrow_blocks",
@@ -548,11 +542,12 @@ def _pobtasi_permuted(D, Lo, Ar, T, buffer, kwargs):
                                       _stream(device))
         _lib.raise_for(rc, "pobtasi")
         _finish(w)
+        _check_status(ws, precision, "pobtasi")
 
 
 def _pobtas_permuted(D, Lo, Ar, T, B, buffer, trans, kwargs):
-    """pobtas(..., buffer=): src/serinv/algs/pobtas.py:164-218."""
-    precision = _native_only(kwargs, "pobtas")
+    """pobtas(..., buffer=): src/serinv/algs/pobtas.py:164-218 (storage precision in either mode)."""
+    precision = _precision(kwargs)
     lib = _lib.load()
     device, w = _prepare((D, Lo, Ar, T, B, buffer),
                          ("L_diagonal_blocks", "L_lower_diagonal_blocks", "L_lower_arrow_blocks",

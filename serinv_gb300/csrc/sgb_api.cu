@@ -125,6 +125,55 @@ cudaError_t ctx_gemm(void* c, GemmProb<T>* pr, int np, cudaStream_t s) {
     return run_gemm<T>(*(const Ctx*)c, pr, np, s);
 }
 
+// Independent problems of up to three terms each.  Natively one SIMT launch.
+// With slices, each problem's terms are cut into groups that fit the
+// tensor-core bound (concatenated K <= kTcMaxK, at most two terms); group g
+// of every problem goes in round g -- the first with the problem's own beta
+// and C_in, the later ones accumulating into C_out -- at most four problems
+// per tensor-core launch.
+template <typename T>
+cudaError_t run_gemm_groups(const Ctx& c, const GemmProb<T>* pr, int np, cudaStream_t s) {
+    if (c.slices == 0) {
+        GemmProb<T> tmp[kMaxProbs];
+        for (int i = 0; i < np; ++i) tmp[i] = pr[i];
+        return gemm_simt<T>(tmp, np, s);
+    }
+    GemmProb<T> rounds[kMaxTerms][kMaxProbs];
+    int nr[kMaxTerms] = {0, 0, 0};
+    for (int i = 0; i < np; ++i) {
+        const GemmProb<T>& p = pr[i];
+        int g = 0, t = 0;
+        while (t < p.nterms || (t == 0 && p.nterms == 0)) {
+            GemmProb<T> q = p;
+            q.nterms = 0;
+            int64_t k = 0;
+            while (t < p.nterms && q.nterms < 2) {
+                const int64_t kp = ceil_div(p.term[t].K, 32) * 32;
+                if (q.nterms > 0 && k + kp > kTcMaxK) break;
+                q.term[q.nterms++] = p.term[t++];
+                k += kp;
+            }
+            if (g > 0) {  // accumulate onto the previous rounds' result
+                q.beta = T(1);
+                q.Cin = q.Cout;
+                q.ldcin = q.ldc;
+                q.strideCin = q.strideC;
+                q.transCin = 0;
+            }
+            rounds[g][nr[g]++] = q;
+            ++g;
+            if (p.nterms == 0) break;
+        }
+    }
+    for (int g = 0; g < kMaxTerms; ++g)
+        for (int i0 = 0; i0 < nr[g]; i0 += 4) {
+            const int cnt = nr[g] - i0 < 4 ? nr[g] - i0 : 4;
+            cudaError_t e = run_gemm<T>(c, rounds[g] + i0, cnt, s);
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
+
 // Tensor-core scratch of the largest grouped product of a batched
 // recursive-doubling inversion of `batch` m x m blocks: at level h, up to
 // four pair problems of h x h (K = h) per launch.
@@ -186,7 +235,7 @@ struct PobtafWs {
         tinv = c.take(sizeof(T) * (10 * kTile * kTile + 9 * kTile));  // column-block kernel scratch
         const int64_t mx = m->b > m->a ? m->b : m->a;
         const int Sm = Si > S ? Si : S;
-        tc_bytes = S ? tc_bound(Sm, mx, m->b, 3) : 0;
+        tc_bytes = S ? tc_bound(Sm, mx, m->b, 4) : 0;  // up to four problems per product launch
         tc = c.take(tc_bytes);
         // mixed precision only: L_ii^{-T} of the current diagonal block
         xinv = c.take(S ? sizeof(T) * m->b * m->b : 0);
@@ -1093,15 +1142,30 @@ GemmProb<T> upd_prob(T* C, int64_t ldc, int64_t M, int64_t N, T alpha, T beta) {
 }
 
 template <typename T>
-int pobtaf_permuted_run(const sgb_bta* m, T* buf, void* ws, int32_t* info, cudaStream_t s) {
+int pobtaf_permuted_run(const sgb_bta* m, T* buf, int S, int Si, void* ws, int32_t* info, cudaStream_t s) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
     T* Ar = (T*)m->arrow;
     T* Tp = (T*)m->tip;
-    PobtafWs<T> L(m, 0);
+    PobtafWs<T> L(m, S, Si);
     T* tinv = (T*)((char*)ws + L.tinv);
+    Ctx cx;
+    cx.slices = S;
+    cx.tc = (char*)ws + L.tc;
+    cx.tc_bytes = L.tc_bytes;
+    cx.status = (int32_t*)((char*)ws + L.status);
+    Ctx cxi = cx;
+    cxi.slices = Si ? Si : S;
+    unsigned* bar = (unsigned*)((char*)ws + L.bar);
+    T* Xinv = (T*)((char*)ws + L.xinv);
     const int64_t bb = b * b, ab = a * b;
+    // mixed: the persistent column-block kernel factors D_i and forms
+    // L_ii^{-T}; the three row sets below become one tensor-core product
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    SGB_TRY(cudaStreamIsCapturing(s, &cap));
+    bool mixed_inverse = S != 0 && (S < 7 || Si != 0) && b > 2 * kTile && cap == cudaStreamCaptureStatusNone;
+    if (mixed_inverse) SGB_TRY(cudaMemsetAsync(Xinv, 0, sizeof(T) * bb, s));
     {   // buf[1] = Lo[0]^T  (pobtaf.py:203)
         GemmProb<T> c = copy_prob<T>(buf + bb, b, Lo, b, b, b);
         c.transCin = 1;
@@ -1110,8 +1174,36 @@ int pobtaf_permuted_run(const sgb_bta* m, T* buf, void* ws, int32_t* info, cudaS
     for (int64_t i = 1; i < n - 1; ++i) {  // :206
         // [D_i; Lo_i; buf_i; Ar_i] <- Cholesky of the column block  (:208-242)
         RowSet<T> r1{Lo + i * bb, b, b}, r2{buf + i * bb, b, b}, r3{a ? Ar + i * ab : nullptr, a, b};
-        cudaError_t e = factor_column_block<T>(D + i * bb, b, b, r1, r2, tinv, info, i * b, s, r3);
-        if (e != cudaSuccess) return cuda_fail(e);
+        bool done = false;
+        if (mixed_inverse) {
+            RowSet<T> none{nullptr, 0, b};
+            cudaError_t e = factor_panel_persistent<T>(D + i * bb, b, b, none, none, tinv, bar, cx.status, info, i * b,
+                                                       s, Xinv, 0);
+            if (e == cudaSuccess) {
+                GemmProb<T> pr[3];
+                int np = 0;
+                for (RowSet<T> r : {r1, r2, r3}) {
+                    if (r.rows <= 0 || r.p == nullptr) continue;
+                    GemmProb<T> p = prob<T>();  // rows <- rows * L_ii^{-T}, in place (operands are sliced first)
+                    p.M = (int32_t)r.rows;
+                    p.N = (int32_t)b;
+                    set_term<T>(p, 0, r.p, r.ld, 0, Xinv, b, 0, b, KM_LT_N1);
+                    p.Cout = r.p;
+                    p.ldc = r.ld;
+                    pr[np++] = p;
+                }
+                SGB_TRY(run_gemm<T>(cxi, pr, np, s));
+                done = true;
+            } else if (e != cudaErrorNotSupported) {
+                return cuda_fail(e);
+            } else {
+                mixed_inverse = false;  // too few SMs for the persistent launch
+            }
+        }
+        if (!done) {
+            cudaError_t e = factor_column_block<T>(D + i * bb, b, b, r1, r2, tinv, info, i * b, s, r3);
+            if (e != cudaSuccess) return cuda_fail(e);
+        }
         GemmProb<T> pr[6];
         int np = 0;
         const T* lo = Lo + i * bb;
@@ -1137,7 +1229,7 @@ int pobtaf_permuted_run(const sgb_bta* m, T* buf, void* ws, int32_t* info, cudaS
             set_term<T>(p, 0, ar, b, 0, bu, b, 1, b);
             pr[np++] = p;
         }
-        SGB_TRY(gemm_simt<T>(pr, np, s));
+        SGB_TRY(run_gemm_groups<T>(cx, pr, np, s));
     }
     return SGB_OK;
 }
@@ -1146,13 +1238,25 @@ int pobtaf_permuted_run(const sgb_bta* m, T* buf, void* ws, int32_t* info, cudaS
 // F_i = buf_i L_ii^{-1}, H_i = Ar_i L_ii^{-1}, and the inversion scratch.
 template <typename T>
 struct PobtasiPermWs {
-    size_t status, linv, trtri, gfh, total;
+    size_t status, linv, trtri, gfh, tc, tc_bytes, total;
     int64_t chunk;
-    explicit PobtasiPermWs(const sgb_bta* m) {
+    explicit PobtasiPermWs(const sgb_bta* m, int S = 0, int Si = 0) {
         const int64_t n = m->n, b = m->b, a = m->a;
         chunk = n < kSiChunk ? (n > 0 ? n : 1) : kSiChunk;
         Carve c;
         status = c.take(256);
+        tc_bytes = 0;
+        if (Si > S) S = Si;
+        if (S) {  // slice scratch of the largest tensor-core launch
+            const int64_t tb = chunk < kSiTcBatch ? chunk : kSiTcBatch;
+            const int64_t mx = b > a ? b : a;
+            size_t need[3];
+            need[0] = 3 * tc_prob_bytes(S, b, b, b, tb) + tc_prob_bytes(S, a, b, b, tb);  // G, F, H, P
+            need[1] = trtri_tc_bytes(S, b, chunk);
+            need[2] = 3 * tc_prob_bytes(S, mx, b, kTcMaxK, 1);  // one round of the back-sweep products
+            for (size_t v : need) tc_bytes = v > tc_bytes ? v : tc_bytes;
+        }
+        tc = c.take(tc_bytes);
         linv = c.take(sizeof(T) * (size_t)(chunk * b * b));
         trtri = c.take(sizeof(T) * trtri_scratch_elems(b, chunk));
         gfh = c.take(sizeof(T) * (size_t)(chunk * (2 * b + a) * b));
@@ -1161,65 +1265,78 @@ struct PobtasiPermWs {
 };
 
 template <typename T>
-int pobtasi_permuted_run(const sgb_bta* m, T* buf, void* ws, cudaStream_t s) {
+int pobtasi_permuted_run(const sgb_bta* m, T* buf, int S, int Si, void* ws, cudaStream_t s) {
     const int64_t n = m->n, b = m->b, a = m->a;
     T* D = (T*)m->diag;
     T* Lo = (T*)m->lower;
     T* Ar = (T*)m->arrow;
     T* Tp = (T*)m->tip;
-    PobtasiPermWs<T> W(m);
+    PobtasiPermWs<T> W(m, S, Si);
     char* base = (char*)ws;
     T* Linv = (T*)(base + W.linv);
     T* trs = (T*)(base + W.trtri);
     T* GFH = (T*)(base + W.gfh);
     const int64_t bb = b * b, ab = a * b, gs = (2 * b + a) * b;
-    Ctx native;
+    Ctx cx;  // native, or tensor-core slice products
+    cx.slices = S;
+    cx.tc = base + W.tc;
+    cx.tc_bytes = W.tc_bytes;
+    cx.status = (int32_t*)(base + W.status);
+    Ctx cxi = cx;  // the inversions and the products with L_ii^{-1}
+    cxi.slices = Si ? Si : S;
     // blocks n-2 .. 1, in chunks from the bottom (pobtasi.py:199)
+    const int64_t tcb = S ? (W.chunk < kSiTcBatch ? W.chunk : kSiTcBatch) : W.chunk;
     for (int64_t hi = n - 1; hi > 1; hi -= W.chunk) {
         const int64_t lo = hi - W.chunk > 1 ? hi - W.chunk : 1;
         const int64_t cnt = hi - lo;
-        SGB_TRY(trtri_run<T>(native, D + lo * bb, b, cnt, Linv, trs, s));
-        // G, F, H from the factor, P = L^{-T} L^{-1} into D_j (L_jj is dead then)
-        GemmProb<T> pr[4];
-        int np = 0;
-        GemmProb<T> p = prob<T>();
-        p.M = p.N = (int32_t)b;
-        p.batch = (int32_t)cnt;
-        set_term<T>(p, 0, Lo + lo * bb, b, 0, Linv, b, 0, b, KM_GE_N0);
-        p.term[0].strideA = bb;
-        p.term[0].strideB = bb;
-        p.Cout = GFH;
-        p.ldc = b;
-        p.strideC = gs;
-        pr[np++] = p;
-        GemmProb<T> q = p;
-        q.term[0].A = buf + lo * bb;
-        q.Cout = GFH + bb;
-        pr[np++] = q;
-        if (a) {
-            GemmProb<T> h = prob<T>();
-            h.M = (int32_t)a;
-            h.N = (int32_t)b;
-            h.batch = (int32_t)cnt;
-            set_term<T>(h, 0, Ar + lo * ab, b, 0, Linv, b, 0, b, KM_GE_N0);
-            h.term[0].strideA = ab;
-            h.term[0].strideB = bb;
-            h.Cout = GFH + 2 * bb;
-            h.ldc = b;
-            h.strideC = gs;
-            pr[np++] = h;
+        SGB_TRY(trtri_run<T>(cxi, D + lo * bb, b, cnt, Linv, trs, s));
+        // G, F, H from the factor, P = L^{-T} L^{-1} into D_j (L_jj is dead
+        // then), tcb blocks per launch
+        for (int64_t j0 = lo; j0 < hi; j0 += tcb) {
+            const int64_t jn = (hi - j0) < tcb ? (hi - j0) : tcb;
+            T* GFHj = GFH + (j0 - lo) * gs;
+            const T* Lj = Linv + (j0 - lo) * bb;
+            GemmProb<T> pr[4];
+            int np = 0;
+            GemmProb<T> p = prob<T>();
+            p.M = p.N = (int32_t)b;
+            p.batch = (int32_t)jn;
+            set_term<T>(p, 0, Lo + j0 * bb, b, 0, Lj, b, 0, b, KM_GE_N0);
+            p.term[0].strideA = bb;
+            p.term[0].strideB = bb;
+            p.Cout = GFHj;
+            p.ldc = b;
+            p.strideC = gs;
+            pr[np++] = p;
+            GemmProb<T> q = p;
+            q.term[0].A = buf + j0 * bb;
+            q.Cout = GFHj + bb;
+            pr[np++] = q;
+            if (a) {
+                GemmProb<T> h = prob<T>();
+                h.M = (int32_t)a;
+                h.N = (int32_t)b;
+                h.batch = (int32_t)jn;
+                set_term<T>(h, 0, Ar + j0 * ab, b, 0, Lj, b, 0, b, KM_GE_N0);
+                h.term[0].strideA = ab;
+                h.term[0].strideB = bb;
+                h.Cout = GFHj + 2 * bb;
+                h.ldc = b;
+                h.strideC = gs;
+                pr[np++] = h;
+            }
+            GemmProb<T> pp = prob<T>();
+            pp.M = pp.N = (int32_t)b;
+            pp.batch = (int32_t)jn;
+            set_term<T>(pp, 0, Lj, b, 1, Lj, b, 0, b, KM_GE_M0);
+            pp.term[0].strideA = bb;
+            pp.term[0].strideB = bb;
+            pp.Cout = D + j0 * bb;
+            pp.ldc = b;
+            pp.strideC = bb;
+            pr[np++] = pp;
+            SGB_TRY(run_gemm_groups<T>(cxi, pr, np, s));
         }
-        GemmProb<T> pp = prob<T>();
-        pp.M = pp.N = (int32_t)b;
-        pp.batch = (int32_t)cnt;
-        set_term<T>(pp, 0, Linv, b, 1, Linv, b, 0, b, KM_GE_M0);
-        pp.term[0].strideA = bb;
-        pp.term[0].strideB = bb;
-        pp.Cout = D + lo * bb;
-        pp.ldc = b;
-        pp.strideC = bb;
-        pr[np++] = pp;
-        SGB_TRY(gemm_simt<T>(pr, np, s));
         for (int64_t i = hi - 1; i >= lo; --i) {
             const T* G = GFH + (i - lo) * gs;
             const T* F = G + bb;
@@ -1243,13 +1360,13 @@ int pobtasi_permuted_run(const sgb_bta* m, T* buf, void* ws, cudaStream_t s) {
                 set_term<T>(x[2], 2, Tp, a, 0, H, b, 0, a);
                 nx = 3;
             }
-            SGB_TRY(gemm_simt<T>(x, nx, s));
+            SGB_TRY(run_gemm_groups<T>(cx, x, nx, s));
             // X_ii = P_i - X_{i+1,i}^T G - X_{top,i}^T F - X_{A,i}^T H  (:234-241)
             GemmProb<T> d = upd_prob<T>(D + i * bb, b, b, b, T(-1), T(1));
             set_term<T>(d, 0, Lo + i * bb, b, 1, G, b, 0, b);
             set_term<T>(d, 1, buf + i * bb, b, 1, F, b, 0, b);
             if (a) set_term<T>(d, 2, Ar + i * ab, b, 1, H, b, 0, a);
-            SGB_TRY(gemm_simt<T>(&d, 1, s));
+            SGB_TRY(run_gemm_groups<T>(cx, &d, 1, s));
         }
     }
     // X_{1,0} = X_{top,1}^T  (:244)
@@ -1698,7 +1815,7 @@ int sgb_pobtaf_permuted(const sgb_bta* m, void* buffer, int precision, void* wor
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
     if (S < 0) return -S;
-    if (S != 0) return SGB_ERR_UNSUPPORTED;
+    const int Si = parse_inv_slices(precision, S);
     if (m->n < 2) return SGB_ERR_SHAPE;
     if (buffer == nullptr) return SGB_ERR_ARG;
     size_t need = 0;
@@ -1706,8 +1823,9 @@ int sgb_pobtaf_permuted(const sgb_bta* m, void* buffer, int precision, void* wor
     if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if (info) SGB_TRY(cudaMemsetAsync(info, 0, sizeof(int32_t), s));
-    if (m->dtype == SGB_F64) return pobtaf_permuted_run<double>(m, (double*)buffer, workspace, info, s);
-    return pobtaf_permuted_run<float>(m, (float*)buffer, workspace, info, s);
+    SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
+    if (m->dtype == SGB_F64) return pobtaf_permuted_run<double>(m, (double*)buffer, S, Si, workspace, info, s);
+    return pobtaf_permuted_run<float>(m, (float*)buffer, S, Si, workspace, info, s);
 }
 
 int sgb_pobtaf_permuted_workspace_size(const sgb_bta* m, int precision, size_t* bytes) {
@@ -1726,9 +1844,9 @@ int sgb_pobtasi_permuted_workspace_size(const sgb_bta* m, int precision, size_t*
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
     if (S < 0) return -S;
-    if (S != 0) return SGB_ERR_UNSUPPORTED;
+    const int Si = parse_inv_slices(precision, S);
     if (!bytes) return SGB_ERR_ARG;
-    *bytes = m->dtype == SGB_F64 ? PobtasiPermWs<double>(m).total : PobtasiPermWs<float>(m).total;
+    *bytes = m->dtype == SGB_F64 ? PobtasiPermWs<double>(m, S, Si).total : PobtasiPermWs<float>(m, S, Si).total;
     return SGB_OK;
 }
 
@@ -1743,15 +1861,16 @@ int sgb_pobtasi_permuted(const sgb_bta* m, void* buffer, int precision, void* wo
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
     if (S < 0) return -S;
-    if (S != 0) return SGB_ERR_UNSUPPORTED;
+    const int Si = parse_inv_slices(precision, S);
     if (m->n < 2) return SGB_ERR_SHAPE;
     if (buffer == nullptr) return SGB_ERR_ARG;
     size_t need = 0;
     sgb_pobtasi_permuted_workspace_size(m, precision, &need);
     if ((rc = check_ws(workspace, workspace_bytes, need))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
-    if (m->dtype == SGB_F64) return pobtasi_permuted_run<double>(m, (double*)buffer, workspace, s);
-    return pobtasi_permuted_run<float>(m, (float*)buffer, workspace, s);
+    SGB_TRY(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));  // status word
+    if (m->dtype == SGB_F64) return pobtasi_permuted_run<double>(m, (double*)buffer, S, Si, workspace, s);
+    return pobtasi_permuted_run<float>(m, (float*)buffer, S, Si, workspace, s);
 }
 
 int sgb_pobtas_permuted(const sgb_bta* m, void* buffer, void* rhs, int64_t nrhs, int64_t ldb, char trans,
@@ -1764,8 +1883,7 @@ int sgb_pobtas_permuted(const sgb_bta* m, void* buffer, void* rhs, int64_t nrhs,
     int rc = check_bta(m);
     if (rc) return rc;
     const int S = parse_precision(precision, m->dtype);
-    if (S < 0) return -S;
-    if (S != 0) return SGB_ERR_UNSUPPORTED;
+    if (S < 0) return -S;  // the solve runs in the storage precision in either mode
     if (trans != 'N' && trans != 'T' && trans != 'C') return SGB_ERR_ARG;
     if (nrhs < 0 || nrhs > (1 << 20) || ldb < nrhs) return SGB_ERR_SHAPE;
     if ((nrhs > 0 && rhs == nullptr) || buffer == nullptr) return SGB_ERR_ARG;

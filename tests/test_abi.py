@@ -98,9 +98,11 @@ def test_permuted_entry_points_host_checks(lib):
     assert lib.sgb_pobtasi_permuted_workspace_size(ctypes.byref(m), 0, ctypes.byref(sz)) == 0
     assert sz.value % 256 == 0 and sz.value >= 4 * 8 * 8 * 8
     mixed = _lib.SGB_PREC_MIXED
-    assert lib.sgb_pobtasi_permuted_workspace_size(ctypes.byref(m), mixed, ctypes.byref(sz)) == \
-        _lib.SGB_ERR_UNSUPPORTED
-    assert lib.sgb_pobtaf_permuted(ctypes.byref(m), 0x1000, mixed, 0x1000, 1 << 30, None, None) == \
+    plain = sz.value
+    assert lib.sgb_pobtasi_permuted_workspace_size(ctypes.byref(m), mixed, ctypes.byref(sz)) == 0
+    assert sz.value > plain  # slice scratch of the mixed form
+    m32 = _desc(n=4, b=8, a=2, dtype=_lib.SGB_F32)
+    assert lib.sgb_pobtaf_permuted(ctypes.byref(m32), 0x1000, mixed, 0x1000, 1 << 30, None, None) == \
         _lib.SGB_ERR_UNSUPPORTED
     assert lib.sgb_pobtaf_permuted(ctypes.byref(m), None, 0, 0x1000, 1 << 30, None, None) == _lib.SGB_ERR_ARG
     assert lib.sgb_pobtaf_permuted(ctypes.byref(m), 0x1000, 0, None, 0, None, None) == _lib.SGB_ERR_WORKSPACE

@@ -35,17 +35,6 @@ def test_pobtas_streaming_not_implemented(m):
         sg.pobtas(*m.arrays(), m.B, device_streaming=True)
 
 
-def test_permuted_mixed_precision_not_implemented(m):
-    """buffer= computes in the storage precision; the slice products are not offered there."""
-    buf = np.empty_like(m.D)
-    with pytest.raises(NotImplementedError):
-        sg.pobtaf(*m.arrays(), buffer=buf, precision="mixed")
-    with pytest.raises(NotImplementedError):
-        sg.pobtasi(*m.arrays(), buffer=buf, precision="mixed")
-    with pytest.raises(NotImplementedError):
-        sg.pobtas(*m.arrays(), m.B, buffer=buf, precision="mixed")
-
-
 def test_permuted_streaming_solve_not_implemented(m):
     """pobtas.py:31-36 and pobts.py:29-32: streaming is refused for the permuted solve."""
     buf = np.empty_like(m.D)

@@ -132,3 +132,28 @@ def test_permuted_rejects_bad_buffer():
         sg.pobtaf(*d, buffer=torch.zeros((4, 8, 4), dtype=torch.float64, device="cuda"))
     with pytest.raises(TypeError):
         sg.pobtaf(*d, buffer=torch.zeros((4, 8, 8), dtype=torch.float32, device="cuda"))
+
+
+@pytest.mark.parametrize("shape", [
+    (70, 128, 16, 2),    # column-block kernel with L_ii^{-T}; crosses the 64-block chunk
+    (5, 512, 64, 2),     # the benchmark's block size: three-term products cut into tensor-core groups
+    (6, 100, 0, 2),      # no arrowhead
+    (6, 64, 8, 2),       # launch-based diagonal tiles, tensor-core products
+])
+def test_permuted_mixed_against_oracle(shape):
+    """The permuted forms in the mixed form (FP64 storage, block products as
+    bf16 slice products on the tensor cores) inside the middle-partition
+    workflow, against the oracle at the mixed-precision bar 1e-9."""
+    n, b, a, r = shape
+    m = generate(n, b, a, r, seed=91 + n + b, dtype=np.float64)
+    got = _run_torch(_lib_fn(precision="mixed"), m.D, m.Lo, m.Ar, m.T, m.B)
+    ref = _run_oracle(m.D, m.Lo, m.Ar, m.T, m.B)
+    _compare(got, ref, 1e-9, n)
+
+
+def test_permuted_mixed_rejects_float32():
+    m = generate(4, 16, 2, 1, seed=3, dtype=np.float32)
+    d = [torch.from_numpy(x).cuda() for x in m.arrays()]
+    buf = torch.zeros_like(d[0])
+    with pytest.raises(NotImplementedError):
+        sg.pobtaf(*d, buffer=buf, precision="mixed")
