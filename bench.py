@@ -55,8 +55,9 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--precision", default="mixed",
                    help="fp64 | mixed | mixed:S (S = slice count 3..7); the headline form")
-    p.add_argument("--compare", default="fp64",
-                   help="comma-separated forms timed beside the headline (empty: none)")
+    p.add_argument("--compare", default="fp64,mixed:7:7",
+                   help="comma-separated forms timed beside the headline (empty: none); mixed:7:7 is the "
+                        "conditioning-robust form (7 slices everywhere)")
     p.add_argument("--n", type=int, default=512)
     p.add_argument("--b", type=int, default=512)
     p.add_argument("--a", type=int, default=64)
