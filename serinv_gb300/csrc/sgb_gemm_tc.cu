@@ -875,10 +875,19 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
     // 128 x 64 tiles.  When they leave most SMs idle, each tile's K range is
     // split over a cluster of ks CTAs (exact FP32 reduction through
     // distributed shared memory); failing that, 128 x 32 tiles.
+    // tiles that do work: above-diagonal tiles of a lower-only product exit
+    // at once and leave their SMs to the K split of the others
     int64_t tiles64 = 0, minkb = 1 << 30;
     for (int i = 0; i < np; ++i)
         if (probs[i].M > 0 && probs[i].N > 0 && probs[i].batch > 0) {
-            tiles64 += ceil_div(probs[i].M, TC_BM) * ceil_div(probs[i].N, kTcBN) * probs[i].batch;
+            const int64_t tm = ceil_div(probs[i].M, TC_BM), tn = ceil_div(probs[i].N, kTcBN);
+            int64_t live = tm * tn;
+            if (probs[i].lower_only) {
+                live = 0;
+                for (int64_t m = 0; m < tm; ++m)
+                    for (int64_t n = 0; n < tn; ++n) live += (n * kTcBN < (m + 1) * TC_BM) ? 1 : 0;
+            }
+            tiles64 += live * probs[i].batch;
             int64_t kp = 0;
             for (int t = 0; t < probs[i].nterms; ++t) kp += ceil_div(probs[i].term[t].K, TC_BK);
             minkb = kp < minkb ? kp : minkb;
