@@ -39,6 +39,10 @@ import time
 
 import numpy as np
 
+# hardware queues for concurrent graph branches (the batch workload); must be
+# set before CUDA initialises -- the library sets the same default on import
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -484,7 +488,7 @@ def bench_batched(args):
 
     import serinv_gb300 as sg
     from serinv_gb300 import _lib
-    from serinv_gb300.batched import BatchPlan, autotune_nstreams
+    from serinv_gb300.batched import BatchPlan, autotune
     from serinv_gb300.synthetic import batch_shapes, generate
 
     torch.cuda.set_device(0)
@@ -503,10 +507,10 @@ def bench_batched(args):
     rhs = [r.clone() for r in rhs0]
     prec = ["mixed" if args.batch_precision == "mixed" else "fp64"] * count
     t0 = time.perf_counter()
-    ns = autotune_nstreams(work, rhs, precisions=prec, candidates=(8, 16, 32, 64), reps=1)
+    ns, panel = autotune(work, rhs, precisions=prec, candidates=(16, 32, 64, 128), reps=1)
     tune_s = time.perf_counter() - t0
     k0 = _lib.launch_count()
-    plan = BatchPlan(work, rhs, precisions=prec, nstreams=ns)
+    plan = BatchPlan(work, rhs, precisions=prec, nstreams=ns, panel_ctas=panel)
     kernels_per_graph = _lib.launch_count() - k0  # launches captured into the plan's graph
 
     def restore():
@@ -555,7 +559,8 @@ def bench_batched(args):
             "dtype": "half f32, half " + ("f64 mixed" if args.batch_precision == "mixed" else "f64"),
             "data": "synthetic (NumPy generator, seed i for matrix i)",
             "config": {"workload": "batch of 256 uneven BTA matrices", "nstreams": ns,
-                       "autotune_s": tune_s, "not_spd": bad},
+                       "panel_ctas": panel or 24, "autotune_s": tune_s, "not_spd": bad,
+                       "hardware_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")},
             "max_rel_err_vs_single_fp64": {**worst, "vs": "single-matrix FP64 GPU path on the same inputs, "
                                                          "max over items of the relative Frobenius error of "
                                                          "each output stack and the solution"},

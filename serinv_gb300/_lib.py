@@ -138,6 +138,10 @@ _SIGNATURES = {
                                              ctypes.POINTER(ctypes.c_int64), ctypes.c_int, ctypes.c_int,
                                              ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_void_p,
                                              ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
+    "sgb_batch_plan_create_ex": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.POINTER(ctypes.c_void_p),
+                                                ctypes.POINTER(ctypes.c_int64), ctypes.c_int, ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
     "sgb_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "sgb_batch_info": (ctypes.c_void_p, [ctypes.c_void_p]),
     "sgb_batch_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -10,10 +10,12 @@ concurrent streams and their sweeps captured into one CUDA graph.
 place exactly as by the single-matrix calls (factor, then the solve with the
 factor, then the selected inversion).
 
-``nstreams=None`` asks the autotuner (``autotune_nstreams``): it times the
-candidate stream counts on scratch copies of the same shapes and caches the
-winner in a JSON file keyed by the batch signature, so the user's data is
-never touched while tuning.
+``nstreams=None`` asks the autotuner (``autotune``): it times candidate
+schedules on scratch copies of the same shapes -- the worker-stream count,
+then the CTA count of the captured column-block launches -- and caches the
+winner in a JSON file keyed by the batch signature, the device and the
+hardware-queue count (``CUDA_DEVICE_MAX_CONNECTIONS``), so the user's data
+is never touched while tuning.
 """
 
 from __future__ import annotations
@@ -29,7 +31,8 @@ from . import _lib
 from .algs import _bta_struct
 
 _OPS = {"pobtaf": 1, "pobtasi": 2, "pobtas": 4}
-CANDIDATES = (4, 8, 16, 32, 64)
+CANDIDATES = (8, 16, 32, 64, 128)
+PANEL_CANDIDATES = (18, 24, 32)
 CACHE = os.environ.get("SGB_AUTOTUNE_CACHE",
                        os.path.join(os.path.expanduser("~"), ".cache", "serinv_gb300", "batch_autotune.json"))
 
@@ -39,12 +42,15 @@ def _signature(mats, rhs, ops, precisions) -> str:
     for i, (D, Lo, Ar, T) in enumerate(mats):
         nr = 0 if rhs is None or rhs[i] is None else rhs[i].shape[1]
         parts.append(f"{D.shape[0]}x{D.shape[1]}x{Ar.shape[1]}:{str(D.dtype)[6:]}:{nr}:{precisions[i]}")
-    key = ";".join(parts) + f"|ops={ops}"
+    dev = torch.cuda.get_device_name(mats[0][0].device) if mats else ""
+    conn = os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8")
+    key = ";".join(parts) + f"|ops={ops}|dev={dev}|conn={conn}"
     return hashlib.sha1(key.encode()).hexdigest()
 
 
 class BatchPlan:
-    def __init__(self, mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None, nstreams=None):
+    def __init__(self, mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None, nstreams=None,
+                 panel_ctas=None):
         self.lib = _lib.load()
         self.mats = [tuple(x.contiguous() for x in m) for m in mats]
         for m in mats:
@@ -59,8 +65,11 @@ class BatchPlan:
                            else _lib.SGB_PREC_NATIVE
                            for p, m in zip(precisions, mats)]
         if nstreams is None:
-            nstreams = autotune_nstreams(mats, rhs, ops, precisions)
+            nstreams, tuned_panel = autotune(mats, rhs, ops, precisions)
+            if panel_ctas is None:
+                panel_ctas = tuned_panel
         self.nstreams = int(nstreams)
+        self.panel_ctas = int(panel_ctas or 0)
         n = len(mats)
         self._descs = (_lib.SgbBta * n)(*[_bta_struct(*m) for m in self.mats])
         self._rhs = (ctypes.c_void_p * n)(*[(r.data_ptr() if r is not None else None)
@@ -75,9 +84,10 @@ class BatchPlan:
         self.ws = torch.empty(nbytes.value, dtype=torch.uint8, device=dev)
         plan = ctypes.c_void_p(0)
         with torch.cuda.device(dev):
-            _lib.raise_for(self.lib.sgb_batch_plan_create(self._descs, self._rhs, self._nrhs, n, self.ops,
-                                                          self._prec, self.nstreams, self.ws.data_ptr(),
-                                                          nbytes.value, ctypes.byref(plan)), "batch plan")
+            _lib.raise_for(self.lib.sgb_batch_plan_create_ex(self._descs, self._rhs, self._nrhs, n, self.ops,
+                                                             self._prec, self.nstreams, self.panel_ctas,
+                                                             self.ws.data_ptr(), nbytes.value, ctypes.byref(plan)),
+                           "batch plan")
         self.plan = plan
         self.device = dev
 
@@ -104,9 +114,38 @@ class BatchPlan:
             pass
 
 
-def autotune_nstreams(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None,
-                      candidates=CANDIDATES, reps: int = 2) -> int:
-    """Pick the stream count by timing scratch copies of the batch; cached by signature."""
+def _time_plan(mats, rhs, scratch, srhs, ops, precisions, ns, panel, reps):
+    """Best of `reps` timed replays of one plan, after an untimed first replay
+    (which also uploads the freshly instantiated graph)."""
+    def restore():
+        for dst, src in zip(scratch, mats):
+            for d, s_ in zip(dst, src):
+                d.copy_(s_)
+        if srhs is not None:
+            for d, s_ in zip(srhs, rhs):
+                if d is not None:
+                    d.copy_(s_)
+
+    plan = BatchPlan(scratch, srhs, ops, precisions, nstreams=ns, panel_ctas=panel)
+    times = []
+    for k in range(reps + 1):
+        restore()
+        st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st.record()
+        plan.run()
+        en.record()
+        en.synchronize()
+        if k > 0:
+            times.append(st.elapsed_time(en))
+    plan.close()
+    return min(times)
+
+
+def autotune(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None, candidates=CANDIDATES,
+             panel_candidates=PANEL_CANDIDATES, reps: int = 2):
+    """Pick (worker-stream count, column-block CTA count) by timing scratch
+    copies of the batch: the stream count first (CTA count 24), then the CTA
+    count at that stream count.  Cached by signature."""
     if precisions is None:
         precisions = ["fp64"] * len(mats)
     opcode = sum(_OPS[o] for o in ops)
@@ -117,39 +156,36 @@ def autotune_nstreams(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), preci
             cache = json.load(f)
     except (OSError, ValueError):
         cache = {}
-    if sig in cache:
-        return int(cache[sig])
+    hit = cache.get(sig)
+    if isinstance(hit, list) and len(hit) == 2:
+        return int(hit[0]), int(hit[1])
     scratch = [tuple(x.clone() for x in m) for m in mats]
     srhs = None if rhs is None else [None if r is None else r.clone() for r in rhs]
-    best, best_t = None, float("inf")
+    best_ns, best_t = None, float("inf")
     for ns in candidates:
-        if ns > max(1, len(mats)) and best is not None:
+        if ns > max(1, len(mats)) and best_ns is not None:
             break
-        times = []
-        for _ in range(reps):
-            for dst, src in zip(scratch, mats):
-                for d, s in zip(dst, src):
-                    d.copy_(s)
-            if srhs is not None:
-                for d, s in zip(srhs, rhs):
-                    if d is not None:
-                        d.copy_(s)
-            plan = BatchPlan(scratch, srhs, ops, precisions, nstreams=ns)
-            st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            st.record()
-            plan.run()
-            en.record()
-            en.synchronize()
-            times.append(st.elapsed_time(en))
-            plan.close()
-        t = min(times)
+        t = _time_plan(mats, rhs, scratch, srhs, ops, precisions, ns, 0, reps)
         if t < best_t:
-            best, best_t = ns, t
-    cache[sig] = best
+            best_ns, best_t = ns, t
+    best_panel = 0
+    for pc in panel_candidates:
+        if pc == 24:  # the stream search ran at 24
+            continue
+        t = _time_plan(mats, rhs, scratch, srhs, ops, precisions, best_ns, pc, reps)
+        if t < best_t:
+            best_panel, best_t = pc, t
+    cache[sig] = [int(best_ns), int(best_panel)]
     try:
         os.makedirs(os.path.dirname(CACHE), exist_ok=True)
         with open(CACHE, "w") as f:
             json.dump(cache, f)
     except OSError:
         pass
-    return int(best)
+    return int(best_ns), int(best_panel)
+
+
+def autotune_nstreams(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None,
+                      candidates=CANDIDATES, reps: int = 2) -> int:
+    """The stream count of ``autotune`` (kept for callers that choose only it)."""
+    return autotune(mats, rhs, ops, precisions, candidates=candidates, reps=reps)[0]

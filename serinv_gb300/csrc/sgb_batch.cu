@@ -16,7 +16,7 @@
 
 #include "sgb_internal.cuh"
 
-// CTAs of a captured column-block launch.
+// CTAs of a captured column-block launch unless the plan asks otherwise.
 constexpr int kPlanPanelGrid = 24;
 
 struct sgb_batch_plan {
@@ -39,7 +39,7 @@ struct Item {
 };
 
 size_t item_ws(const Item& it, int ops) {
-    // sized as the plan's capture runs the item (its panel grid set)
+    // sized as the plan's capture runs the item (a panel grid set)
     sgb::set_capture_panel_grid(kPlanPanelGrid);
     const size_t need = sgb::plan_item_ws(&it.m, ops, it.precision, it.nrhs);
     sgb::set_capture_panel_grid(0);
@@ -135,7 +135,16 @@ int sgb_batch_workspace_size(const sgb_bta* mats, void* const* rhs, const int64_
 int sgb_batch_plan_create(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int count, int ops,
                           const int* precisions, int nstreams, void* workspace, size_t workspace_bytes,
                           sgb_batch_plan** out) {
+    return sgb_batch_plan_create_ex(mats, rhs, nrhs, count, ops, precisions, nstreams, 0, workspace,
+                                    workspace_bytes, out);
+}
+
+int sgb_batch_plan_create_ex(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int count, int ops,
+                             const int* precisions, int nstreams, int panel_ctas, void* workspace,
+                             size_t workspace_bytes, sgb_batch_plan** out) {
     if (!out || nstreams < 1 || nstreams > 256) return SGB_ERR_ARG;
+    if (panel_ctas < 0 || panel_ctas > 1024) return SGB_ERR_ARG;
+    const int pgrid = panel_ctas == 0 ? kPlanPanelGrid : panel_ctas;
     *out = nullptr;
     std::vector<Item> items;
     int rc = validate(mats, rhs, nrhs, count, ops, precisions, items);
@@ -165,9 +174,10 @@ int sgb_batch_plan_create(const sgb_bta* mats, void* const* rhs, const int64_t* 
         capturing = e == cudaSuccess;
     }
     // pobtaf blocks of b > 64 become one cooperative column-block launch of
-    // kPlanPanelGrid CTAs each (a few run side by side); smaller blocks keep
-    // the launch-based tile sweep
-    sgb::set_capture_panel_grid(kPlanPanelGrid);
+    // pgrid CTAs each (a few run side by side; a grid too small for the
+    // kernel's roles falls back to the launch-based tile sweep); smaller
+    // blocks keep the tile sweep
+    sgb::set_capture_panel_grid(pgrid);
     if (e == cudaSuccess) e = cudaEventRecord(events[ns], origin);
     for (int k = 0; k < ns && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(streams[k], events[ns], 0);
     // enqueue every matrix on its stream, biggest first within a stream

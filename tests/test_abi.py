@@ -218,3 +218,14 @@ def test_stream_workspace_does_not_grow_with_n(lib):
     assert lib.sgb_pobtaf_stream_workspace_size(ctypes.byref(m), 0, 1, ctypes.byref(sz)) == _lib.SGB_ERR_SHAPE
     cm = _desc(n=100, b=64, a=8, dtype=_lib.SGB_C128)
     assert lib.sgb_pobtaf_stream_workspace_size(ctypes.byref(cm), 0, 4, ctypes.byref(sz)) == _lib.SGB_ERR_UNSUPPORTED
+
+
+def test_batch_plan_ex_rejects_bad_panel_ctas(lib):
+    m = _desc(n=4, b=8, a=2)
+    plan = ctypes.c_void_p(0)
+    ns = (ctypes.c_int64 * 1)(0)
+    rhs = (ctypes.c_void_p * 1)(None)
+    assert lib.sgb_batch_plan_create_ex(ctypes.byref(m), rhs, ns, 1, 1, None, 1, -1, 0x1000, 1 << 20,
+                                        ctypes.byref(plan)) == _lib.SGB_ERR_ARG
+    assert lib.sgb_batch_plan_create_ex(ctypes.byref(m), rhs, ns, 1, 1, None, 0, 24, 0x1000, 1 << 20,
+                                        ctypes.byref(plan)) == _lib.SGB_ERR_ARG

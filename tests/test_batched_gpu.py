@@ -155,3 +155,39 @@ def test_batch_with_complex_matrices():
                 assert rel_err(got.cpu().numpy(), ref) <= tol[m.D.dtype]
         assert rel_err(r.cpu().numpy(), x) <= tol[m.D.dtype]
     plan.close()
+
+
+def test_plan_panel_cta_counts_agree_with_the_oracle():
+    """The column-block CTA count is a schedule choice only: 18, 32 and a
+    count too small for the kernel's roles (the launch-based tile sweep)
+    give the oracle's results."""
+    rng = np.random.default_rng(33)
+    mats = []
+    for i in range(4):
+        n = int(rng.integers(3, 7))
+        b = int(rng.choice([96, 128]))
+        mats.append(generate(n, b, 8, 2, seed=400 + i, dtype=np.float64))
+    refs = [oracle_run(m) for m in mats]
+    for panel in (18, 32, 4):
+        dev = [tuple(torch.from_numpy(x.copy()).cuda() for x in m.arrays()) for m in mats]
+        rhs = [torch.from_numpy(m.B.copy()).cuda() for m in mats]
+        plan = BatchPlan(dev, rhs, nstreams=2, panel_ctas=panel)
+        plan.run()
+        torch.cuda.synchronize()
+        assert torch.all(plan.info() == 0)
+        for (L, X, x), d, r in zip(refs, dev, rhs):
+            for got, ref in zip(d, X):
+                if ref.size:
+                    assert rel_err(got.cpu().numpy(), ref) <= 1e-12, panel
+            assert rel_err(r.cpu().numpy(), x) <= 1e-12, panel
+        plan.close()
+
+
+def test_autotuner_returns_streams_and_panel_ctas(tmp_path, monkeypatch):
+    import serinv_gb300.batched as bm
+    monkeypatch.setattr(bm, "CACHE", str(tmp_path / "tune.json"))
+    mats = make_batch(4, seed=12)
+    dev = [tuple(torch.from_numpy(x).cuda() for x in m.arrays()) for m in mats]
+    ns, panel = bm.autotune(dev, None, ops=("pobtaf", "pobtasi"), candidates=(1, 2), panel_candidates=(18, 24))
+    assert ns in (1, 2) and panel in (0, 18)
+    assert bm.autotune(dev, None, ops=("pobtaf", "pobtasi")) == (ns, panel)  # cached
