@@ -286,6 +286,20 @@ int sgb_dgemm(int precision, char transA, char transB, int64_t M, int64_t N, int
               const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
               int64_t ldc, void* workspace, size_t workspace_bytes, void* stream);
 
+/*
+ * Backward of logdet(A) + sum_k y_k^T A^{-1} y_k (no counterpart in the
+ * reference, which has no differentiation): X holds the selected inverse of
+ * A from sgb_pobtasi, x = A^{-1} y is (n*b + a, nrhs) row-major with leading
+ * dimension ldx, g points to the upstream gradient (one element of X's
+ * dtype, device memory).  In place, X becomes g * dL/d(stored lower stacks):
+ * (A^{-1} - x x^T) on the pattern, doubled where a stored entry stands for
+ * two entries of the symmetric matrix (strictly-lower entries of diag and
+ * tip, every entry of lower and arrow), zero above the diagonal of diag and
+ * tip.  Real dtypes; one memory-bound pass, no workspace.
+ */
+int sgb_bta_logdet_quad_grad(const sgb_bta* X, const void* x, int64_t nrhs, int64_t ldx, const void* g,
+                             void* stream);
+
 /* ---- batches of independent matrices ------------------------------------
  * Many BTA matrices of uneven n, b, a and dtype processed by one graph
  * launch (no counterpart in the reference, which handles one matrix per

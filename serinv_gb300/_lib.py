@@ -121,6 +121,8 @@ _SIGNATURES = {
     "sgb_pobtas_refine": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.POINTER(SgbBta), ctypes.c_void_p,
                                          ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
                                          ctypes.c_size_t, ctypes.c_void_p]),
+    "sgb_bta_logdet_quad_grad": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.c_void_p, ctypes.c_int64,
+                                                ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
     "sgb_dgemm_workspace_size": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                                 ctypes.POINTER(ctypes.c_size_t)]),
     "sgb_dgemm": (ctypes.c_int, [ctypes.c_int, ctypes.c_char, ctypes.c_char, ctypes.c_int64, ctypes.c_int64,

@@ -14,30 +14,19 @@ mapped to the parameterisation: an entry of a stored lower block stands for
 two entries of the symmetric matrix, so strictly-lower entries of ``D`` and
 ``T`` and every entry of ``Lo`` and ``Ar`` get twice the symmetric-matrix
 gradient; strictly-upper entries of ``D`` and ``T`` (never read) get zero.
-``dL/dy = 2 x``.
+That mapping, the pattern blocks of ``x x^T`` and the scaling by the
+upstream gradient run as one in-place pass over the selected inverse
+(``sgb_bta_logdet_quad_grad``).  ``dL/dy = 2 x``.
 """
 
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
-from .algs import pobtaf, pobtas, pobtasi
-
-
-def _pattern_outer(x: torch.Tensor, n: int, b: int, a: int):
-    """Blocks of x x^T on the BTA pattern (x: (N, k); sums over the k columns)."""
-    xb = x[: n * b].reshape(n, b, -1)
-    xt = x[n * b:]
-    oD = torch.bmm(xb, xb.transpose(1, 2))
-    oLo = torch.bmm(xb[1:], xb[:-1].transpose(1, 2)) if n > 1 else xb.new_zeros((0, b, b))
-    oAr = torch.matmul(xt.unsqueeze(0), xb.transpose(1, 2)) if a else xb.new_zeros((n, 0, b))
-    oT = xt @ xt.T if a else xb.new_zeros((0, 0))
-    return oD, oLo, oAr, oT
-
-
-def _sym_param(G: torch.Tensor) -> torch.Tensor:
-    """Gradient w.r.t. a stored lower triangle: 2 G below, G on, 0 above the diagonal."""
-    return torch.tril(G, -1) * 2.0 + torch.diag_embed(torch.diagonal(G, dim1=-2, dim2=-1))
+from . import _lib
+from .algs import _bta_struct, pobtaf, pobtas, pobtasi
 
 
 class BTALogdetQuad(torch.autograd.Function):
@@ -62,20 +51,17 @@ class BTALogdetQuad(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         L0, L1, L2, L3, x = ctx.saved_tensors
-        n, b, a = L0.shape[0], L0.shape[1], L2.shape[1]
         X = [t.clone() for t in (L0, L1, L2, L3)]
         pobtasi(*X, precision=ctx.precision)  # A^{-1} on the pattern
-        oD, oLo, oAr, oT = _pattern_outer(x, n, b, a)
-        GD = X[0] - oD
-        GLo = X[1] - oLo
-        GAr = X[2] - oAr
-        GT = X[3] - oT
-        dD = _sym_param(GD) * g
-        dLo = 2.0 * GLo * g
-        dAr = 2.0 * GAr * g
-        dT = (_sym_param(GT) if a else GT) * g
+        # in place: X <- g * (A^{-1} - x x^T) on the pattern, mapped to the stored lower stacks
+        gs = g.detach().to(device=x.device, dtype=x.dtype).reshape(1).contiguous()
+        m = _bta_struct(*X)
+        with torch.cuda.device(x.device):
+            rc = _lib.load().sgb_bta_logdet_quad_grad(ctypes.byref(m), x.data_ptr(), x.shape[1], x.shape[1],
+                                                       gs.data_ptr(), torch.cuda.current_stream(x.device).cuda_stream)
+        _lib.raise_for(rc, "logdet/quadratic-form backward")
         dy = (2.0 * x * g).reshape(ctx.yshape)
-        return dD, dLo, dAr, dT, dy, None
+        return X[0], X[1], X[2], X[3], dy, None
 
 
 def bta_logdet_quad(D, Lo, Ar, T, y, precision: str = "fp64") -> torch.Tensor:

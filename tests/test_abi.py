@@ -229,3 +229,12 @@ def test_batch_plan_ex_rejects_bad_panel_ctas(lib):
                                         ctypes.byref(plan)) == _lib.SGB_ERR_ARG
     assert lib.sgb_batch_plan_create_ex(ctypes.byref(m), rhs, ns, 1, 1, None, 0, 24, 0x1000, 1 << 20,
                                         ctypes.byref(plan)) == _lib.SGB_ERR_ARG
+
+
+def test_logdet_grad_host_checks(lib):
+    m = _desc(n=4, b=8, a=2)
+    assert lib.sgb_bta_logdet_quad_grad(ctypes.byref(m), None, 1, 1, 0x1000, None) == _lib.SGB_ERR_ARG
+    assert lib.sgb_bta_logdet_quad_grad(ctypes.byref(m), 0x1000, 0, 1, 0x1000, None) == _lib.SGB_ERR_SHAPE
+    assert lib.sgb_bta_logdet_quad_grad(ctypes.byref(m), 0x1000, 2, 1, 0x1000, None) == _lib.SGB_ERR_SHAPE
+    c = _desc(n=4, b=8, a=2, dtype=_lib.SGB_C128)
+    assert lib.sgb_bta_logdet_quad_grad(ctypes.byref(c), 0x1000, 1, 1, 0x1000, None) == _lib.SGB_ERR_DTYPE

@@ -50,10 +50,11 @@ def make(n, b, a, seed, k=1):
     return ts, y
 
 
-@pytest.mark.parametrize("shape", [(4, 8, 3), (16, 32, 8), (3, 40, 0)])
+@pytest.mark.parametrize("shape", [(4, 8, 3, 1), (16, 32, 8, 1), (3, 40, 0, 1), (5, 24, 4, 3),
+                                   (16, 256, 32, 1)])  # the last: the benchmark's b and a at n = 16
 def test_against_dense_autograd(shape):
-    n, b, a = shape
-    ts, y = make(n, b, a, seed=n + b)
+    n, b, a, k = shape
+    ts, y = make(n, b, a, seed=n + b, k=k)
     loss = bta_logdet_quad(*ts, y)
     loss.backward()
     ours = [t.grad.clone() for t in ts] + [y.grad.clone()]
@@ -98,3 +99,35 @@ def test_central_finite_differences():
         fd = (fp - fm) / (2 * h)
         g = float(t.grad[idx])
         assert abs(fd - g) <= 1e-5 * max(1.0, abs(g)), (which, idx, fd, g)
+
+
+def test_central_finite_differences_at_benchmark_size():
+    """n=1024, b=256, a=32 (N = 262,176): 64 seeded entries of the four
+    stacks, central differences with h = 1e-6 against the selected-inversion
+    gradient.  The loss is ~1e6, so the difference quotient's rounding floor
+    is ~eps |loss| / h ~ 2e-4; the bar is 1e-3 relative to max(1, |g|)."""
+    n, b, a = 1024, 256, 32
+    ts, y = make(n, b, a, seed=0)
+    loss = bta_logdet_quad(*ts, y)
+    loss.backward()
+    rng = np.random.default_rng(0)
+    h = 1e-6
+    base = [x.detach().clone() for x in ts]
+    worst = 0.0
+    for _ in range(64):
+        which = int(rng.integers(0, 4))
+        t = ts[which]
+        idx = tuple(int(rng.integers(0, s_)) for s_ in t.shape)
+        if which in (0, 3) and idx[-1] > idx[-2]:
+            idx = idx[:-2] + (idx[-1], idx[-2])
+        with torch.no_grad():
+            old = float(base[which][idx])
+            base[which][idx] = old + h
+            fp = float(bta_logdet_quad(*base, y.detach()))
+            base[which][idx] = old - h
+            fm = float(bta_logdet_quad(*base, y.detach()))
+            base[which][idx] = old
+        g = float(t.grad[idx])
+        dev = abs((fp - fm) / (2 * h) - g) / max(1.0, abs(g))
+        worst = max(worst, dev)
+    assert worst <= 1e-3, worst
