@@ -53,8 +53,14 @@ namespace {
 constexpr int TC_BM = 128;
 constexpr int TC_BK = 32;
 constexpr int kMaxTcProbs = 4;
-constexpr int64_t kTcSmCount = 148;  // CTAs one launch should keep busy (152 SMs)
-constexpr int kTcMaxSplit = 4;      // CTAs per cluster of a K-split tile
+#ifndef SGB_TC_SM_COUNT
+#define SGB_TC_SM_COUNT 148
+#endif
+#ifndef SGB_TC_MAX_SPLIT
+#define SGB_TC_MAX_SPLIT 4
+#endif
+constexpr int64_t kTcSmCount = SGB_TC_SM_COUNT;  // CTAs one launch should keep busy (152 SMs)
+constexpr int kTcMaxSplit = SGB_TC_MAX_SPLIT;    // CTAs per cluster of a K-split tile (<= 8)
 constexpr int kMaxSplitJobs = 2 * kMaxTcProbs;  // probs x operands
 constexpr long long kSpinLimit = 1ll << 22;         // bounded drain waits after an error (~1 s)
 
