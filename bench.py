@@ -399,13 +399,32 @@ def bench_ours(args, rank: int, world: int, dist):
     # (which the test suite pins to the reference at <= 1e-12)
     acc = {}
     if prec.startswith("mixed") and not args.bare:
+        def rel(x, y):
+            return float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
+
         ref = [x.clone() for x in A0]
         sg.pobtaf(*ref)
+        Lref = [x.clone() for x in ref]
         sg.pobtasi(*ref)
         for name, x, y in zip(("diag", "lower", "arrow", "tip"), A, ref):
-            acc[name] = float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
-        acc["vs"] = "FP64 drop-in on the same inputs (relative Frobenius error per stack)"
-        del ref
+            acc[name] = rel(x, y)
+        acc["vs"] = "FP64 drop-in on the same inputs (relative Frobenius error per stack of the selected inverse)"
+        # the factor L and the solution x of the benchmark's right-hand sides
+        Lm = [x.clone() for x in A0]
+        sg.pobtaf(*Lm, precision=prec)
+        acc["factor"] = {nm: rel(x, y) for nm, x, y in zip(("diag", "lower", "arrow", "tip"), Lm, Lref)}
+        Bh = torch.from_numpy(m.B).cuda()
+        xr = Bh.clone()
+        sg.pobtas(*Lref, xr, trans="N")
+        sg.pobtas(*Lref, xr, trans="T")
+        xm = Bh.clone()
+        sg.pobtas(*Lm, xm, trans="N")
+        sg.pobtas(*Lm, xm, trans="T")
+        xf = Bh.clone()
+        sg.pobtas_refine(*A0, *Lm, xf, iters=1)
+        acc["solution"] = {"nrhs": int(Bh.shape[1]), "mixed_factor": rel(xm, xr),
+                           "mixed_factor_refined_once": rel(xf, xr)}
+        del ref, Lref, Lm
     else:
         acc = {"note": "FP64 path; parity with the reference pinned at <=1e-12 by the test suite"}
 
@@ -507,10 +526,10 @@ def bench_batched(args):
     rhs = [r.clone() for r in rhs0]
     prec = ["mixed" if args.batch_precision == "mixed" else "fp64"] * count
     t0 = time.perf_counter()
-    ns, panel = autotune(work, rhs, precisions=prec, candidates=(16, 32, 64, 128), reps=1)
+    ns, panel, split = autotune(work, rhs, precisions=prec, candidates=(16, 32, 64, 128), reps=1)
     tune_s = time.perf_counter() - t0
     k0 = _lib.launch_count()
-    plan = BatchPlan(work, rhs, precisions=prec, nstreams=ns, panel_ctas=panel)
+    plan = BatchPlan(work, rhs, precisions=prec, nstreams=ns, panel_ctas=panel, tc_ksplit=split)
     kernels_per_graph = _lib.launch_count() - k0  # launches captured into the plan's graph
 
     def restore():
@@ -559,7 +578,7 @@ def bench_batched(args):
             "dtype": "half f32, half " + ("f64 mixed" if args.batch_precision == "mixed" else "f64"),
             "data": "synthetic (NumPy generator, seed i for matrix i)",
             "config": {"workload": "batch of 256 uneven BTA matrices", "nstreams": ns,
-                       "panel_ctas": panel or 24, "autotune_s": tune_s, "not_spd": bad,
+                       "panel_ctas": panel or 24, "tc_ksplit": split, "autotune_s": tune_s, "not_spd": bad,
                        "hardware_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")},
             "max_rel_err_vs_single_fp64": {**worst, "vs": "single-matrix FP64 GPU path on the same inputs, "
                                                          "max over items of the relative Frobenius error of "

@@ -325,15 +325,18 @@ int sgb_batch_workspace_size(const sgb_bta* mats, void* const* rhs, const int64_
 int sgb_batch_plan_create(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int count, int ops,
                           const int* precisions, int nstreams, void* workspace, size_t workspace_bytes,
                           sgb_batch_plan** plan);
-/* As sgb_batch_plan_create, with the CTA count of the captured column-block
- * launches as a tuning parameter: 0 selects 24; a count too small for the
- * kernel's roles (< 18) makes those blocks take the launch-based tile sweep.
- * The workspace size does not depend on it.  Best used with
- * CUDA_DEVICE_MAX_CONNECTIONS >= 32 in the environment (set before the CUDA
- * context exists): the replay's independent branches share that many
- * hardware queues. */
+/* As sgb_batch_plan_create, with two schedule parameters for an autotuner:
+ * panel_ctas, the CTA count of the captured column-block launches (0
+ * selects 24; a count too small for the kernel's roles, < 18, makes those
+ * blocks take the launch-based tile sweep), and options: SGB_BATCH_TC_KSPLIT
+ * lets the captured tensor-core products split K over thread-block clusters
+ * (off by default: the other streams fill the GPU).  The workspace size
+ * depends on neither.  Best used with CUDA_DEVICE_MAX_CONNECTIONS >= 32 in
+ * the environment (set before the CUDA context exists): the replay's
+ * independent branches share that many hardware queues. */
+#define SGB_BATCH_TC_KSPLIT 1
 int sgb_batch_plan_create_ex(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int count, int ops,
-                             const int* precisions, int nstreams, int panel_ctas, void* workspace,
+                             const int* precisions, int nstreams, int panel_ctas, int options, void* workspace,
                              size_t workspace_bytes, sgb_batch_plan** plan);
 int sgb_batch_run(sgb_batch_plan* plan, void* stream);
 const int32_t* sgb_batch_info(const sgb_batch_plan* plan);

@@ -29,6 +29,8 @@ SGB_F64 = 1
 SGB_C64 = 2
 SGB_C128 = 3
 
+SGB_BATCH_TC_KSPLIT = 1
+
 SGB_PREC_NATIVE = 0
 SGB_PREC_MIXED = 1
 
@@ -143,7 +145,8 @@ _SIGNATURES = {
     "sgb_batch_plan_create_ex": (ctypes.c_int, [ctypes.POINTER(SgbBta), ctypes.POINTER(ctypes.c_void_p),
                                                 ctypes.POINTER(ctypes.c_int64), ctypes.c_int, ctypes.c_int,
                                                 ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
-                                                ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
+                                                ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
+                                                ctypes.POINTER(ctypes.c_void_p)]),
     "sgb_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "sgb_batch_info": (ctypes.c_void_p, [ctypes.c_void_p]),
     "sgb_batch_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -12,10 +12,11 @@ factor, then the selected inversion).
 
 ``nstreams=None`` asks the autotuner (``autotune``): it times candidate
 schedules on scratch copies of the same shapes -- the worker-stream count,
-then the CTA count of the captured column-block launches -- and caches the
-winner in a JSON file keyed by the batch signature, the device and the
-hardware-queue count (``CUDA_DEVICE_MAX_CONNECTIONS``), so the user's data
-is never touched while tuning.
+then the CTA count of the captured column-block launches, then whether the
+tensor-core products split K over clusters -- and caches the winner in a
+JSON file keyed by the batch signature, the device and the hardware-queue
+count (``CUDA_DEVICE_MAX_CONNECTIONS``), so the user's data is never
+touched while tuning.
 """
 
 from __future__ import annotations
@@ -50,7 +51,7 @@ def _signature(mats, rhs, ops, precisions) -> str:
 
 class BatchPlan:
     def __init__(self, mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None, nstreams=None,
-                 panel_ctas=None):
+                 panel_ctas=None, tc_ksplit=None):
         self.lib = _lib.load()
         self.mats = [tuple(x.contiguous() for x in m) for m in mats]
         for m in mats:
@@ -65,11 +66,14 @@ class BatchPlan:
                            else _lib.SGB_PREC_NATIVE
                            for p, m in zip(precisions, mats)]
         if nstreams is None:
-            nstreams, tuned_panel = autotune(mats, rhs, ops, precisions)
+            nstreams, tuned_panel, tuned_split = autotune(mats, rhs, ops, precisions)
             if panel_ctas is None:
                 panel_ctas = tuned_panel
+            if tc_ksplit is None:
+                tc_ksplit = tuned_split
         self.nstreams = int(nstreams)
         self.panel_ctas = int(panel_ctas or 0)
+        self.options = _lib.SGB_BATCH_TC_KSPLIT if tc_ksplit else 0
         n = len(mats)
         self._descs = (_lib.SgbBta * n)(*[_bta_struct(*m) for m in self.mats])
         self._rhs = (ctypes.c_void_p * n)(*[(r.data_ptr() if r is not None else None)
@@ -86,7 +90,8 @@ class BatchPlan:
         with torch.cuda.device(dev):
             _lib.raise_for(self.lib.sgb_batch_plan_create_ex(self._descs, self._rhs, self._nrhs, n, self.ops,
                                                              self._prec, self.nstreams, self.panel_ctas,
-                                                             self.ws.data_ptr(), nbytes.value, ctypes.byref(plan)),
+                                                             self.options, self.ws.data_ptr(), nbytes.value,
+                                                             ctypes.byref(plan)),
                            "batch plan")
         self.plan = plan
         self.device = dev
@@ -114,7 +119,7 @@ class BatchPlan:
             pass
 
 
-def _time_plan(mats, rhs, scratch, srhs, ops, precisions, ns, panel, reps):
+def _time_plan(mats, rhs, scratch, srhs, ops, precisions, ns, panel, reps, split=False):
     """Best of `reps` timed replays of one plan, after an untimed first replay
     (which also uploads the freshly instantiated graph)."""
     def restore():
@@ -126,7 +131,7 @@ def _time_plan(mats, rhs, scratch, srhs, ops, precisions, ns, panel, reps):
                 if d is not None:
                     d.copy_(s_)
 
-    plan = BatchPlan(scratch, srhs, ops, precisions, nstreams=ns, panel_ctas=panel)
+    plan = BatchPlan(scratch, srhs, ops, precisions, nstreams=ns, panel_ctas=panel, tc_ksplit=split)
     times = []
     for k in range(reps + 1):
         restore()
@@ -143,9 +148,10 @@ def _time_plan(mats, rhs, scratch, srhs, ops, precisions, ns, panel, reps):
 
 def autotune(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None, candidates=CANDIDATES,
              panel_candidates=PANEL_CANDIDATES, reps: int = 2):
-    """Pick (worker-stream count, column-block CTA count) by timing scratch
-    copies of the batch: the stream count first (CTA count 24), then the CTA
-    count at that stream count.  Cached by signature."""
+    """Pick (worker-stream count, column-block CTA count, tensor-core K
+    split) by timing warm replays on scratch copies of the batch: the stream
+    count first (CTA count 24, no K split), then the CTA count at that
+    stream count, then the K split.  Cached by signature."""
     if precisions is None:
         precisions = ["fp64"] * len(mats)
     opcode = sum(_OPS[o] for o in ops)
@@ -157,8 +163,8 @@ def autotune(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=Non
     except (OSError, ValueError):
         cache = {}
     hit = cache.get(sig)
-    if isinstance(hit, list) and len(hit) == 2:
-        return int(hit[0]), int(hit[1])
+    if isinstance(hit, list) and len(hit) == 3:
+        return int(hit[0]), int(hit[1]), bool(hit[2])
     scratch = [tuple(x.clone() for x in m) for m in mats]
     srhs = None if rhs is None else [None if r is None else r.clone() for r in rhs]
     best_ns, best_t = None, float("inf")
@@ -175,14 +181,18 @@ def autotune(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=Non
         t = _time_plan(mats, rhs, scratch, srhs, ops, precisions, best_ns, pc, reps)
         if t < best_t:
             best_panel, best_t = pc, t
-    cache[sig] = [int(best_ns), int(best_panel)]
+    best_split = False
+    t = _time_plan(mats, rhs, scratch, srhs, ops, precisions, best_ns, best_panel, reps, split=True)
+    if t < best_t:
+        best_split, best_t = True, t
+    cache[sig] = [int(best_ns), int(best_panel), bool(best_split)]
     try:
         os.makedirs(os.path.dirname(CACHE), exist_ok=True)
         with open(CACHE, "w") as f:
             json.dump(cache, f)
     except OSError:
         pass
-    return int(best_ns), int(best_panel)
+    return int(best_ns), int(best_panel), bool(best_split)
 
 
 def autotune_nstreams(mats, rhs=None, ops=("pobtaf", "pobtasi", "pobtas"), precisions=None,

@@ -135,15 +135,16 @@ int sgb_batch_workspace_size(const sgb_bta* mats, void* const* rhs, const int64_
 int sgb_batch_plan_create(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int count, int ops,
                           const int* precisions, int nstreams, void* workspace, size_t workspace_bytes,
                           sgb_batch_plan** out) {
-    return sgb_batch_plan_create_ex(mats, rhs, nrhs, count, ops, precisions, nstreams, 0, workspace,
+    return sgb_batch_plan_create_ex(mats, rhs, nrhs, count, ops, precisions, nstreams, 0, 0, workspace,
                                     workspace_bytes, out);
 }
 
 int sgb_batch_plan_create_ex(const sgb_bta* mats, void* const* rhs, const int64_t* nrhs, int count, int ops,
-                             const int* precisions, int nstreams, int panel_ctas, void* workspace,
+                             const int* precisions, int nstreams, int panel_ctas, int options, void* workspace,
                              size_t workspace_bytes, sgb_batch_plan** out) {
     if (!out || nstreams < 1 || nstreams > 256) return SGB_ERR_ARG;
     if (panel_ctas < 0 || panel_ctas > 1024) return SGB_ERR_ARG;
+    if ((options & ~SGB_BATCH_TC_KSPLIT) != 0) return SGB_ERR_ARG;
     const int pgrid = panel_ctas == 0 ? kPlanPanelGrid : panel_ctas;
     *out = nullptr;
     std::vector<Item> items;
@@ -178,6 +179,7 @@ int sgb_batch_plan_create_ex(const sgb_bta* mats, void* const* rhs, const int64_
     // kernel's roles falls back to the launch-based tile sweep); smaller
     // blocks keep the tile sweep
     sgb::set_capture_panel_grid(pgrid);
+    sgb::set_capture_tc_split((options & SGB_BATCH_TC_KSPLIT) != 0);
     if (e == cudaSuccess) e = cudaEventRecord(events[ns], origin);
     for (int k = 0; k < ns && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(streams[k], events[ns], 0);
     // enqueue every matrix on its stream, biggest first within a stream
@@ -198,6 +200,7 @@ int sgb_batch_plan_create_ex(const sgb_bta* mats, void* const* rhs, const int64_
         if (e == cudaSuccess) e = cudaStreamWaitEvent(origin, events[k], 0);
     }
     sgb::set_capture_panel_grid(0);
+    sgb::set_capture_tc_split(false);
     if (capturing) {
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(origin, &g);

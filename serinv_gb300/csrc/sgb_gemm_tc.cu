@@ -900,7 +900,7 @@ cudaError_t gemm_tc(GemmProb<double>* probs, int np, int S, void* ws, size_t ws_
         }
     int ks = 1;
     // a launch captured beside other streams' work keeps one CTA per tile
-    const bool shared_gpu = capture_panel_grid() > 0 && capturing(s);
+    const bool shared_gpu = capture_panel_grid() > 0 && capturing(s) && !capture_tc_split();
     if (tiles64 > 0 && tiles64 < 100 && !shared_gpu) {
         int64_t k = kTcSmCount / tiles64;
         if (k > kTcMaxSplit) k = kTcMaxSplit;

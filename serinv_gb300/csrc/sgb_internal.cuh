@@ -129,6 +129,10 @@ cudaError_t factor_panel_persistent(T* diag, int64_t m, int64_t ldd, RowSet<T> r
 // streams (no K split across clusters).
 void set_capture_panel_grid(int ctas);
 int capture_panel_grid();
+// Whether tensor-core products captured beside other streams (a batch
+// plan) may split K over clusters; off unless the plan asks for it.
+void set_capture_tc_split(bool on);
+bool capture_tc_split();
 
 // Full triangular inverse of `batch` lower-triangular m x m blocks:
 // Linv_j = L_j^{-1} (zeros above the diagonal).  Scratch: batch*m*m T.

@@ -693,4 +693,10 @@ thread_local int t_capture_panel_grid = 0;
 void set_capture_panel_grid(int ctas) { t_capture_panel_grid = ctas < 0 ? 0 : ctas; }
 int capture_panel_grid() { return t_capture_panel_grid; }
 
+namespace {
+thread_local bool t_capture_tc_split = false;
+}
+void set_capture_tc_split(bool on) { t_capture_tc_split = on; }
+bool capture_tc_split() { return t_capture_tc_split; }
+
 }  // namespace sgb

@@ -225,9 +225,11 @@ def test_batch_plan_ex_rejects_bad_panel_ctas(lib):
     plan = ctypes.c_void_p(0)
     ns = (ctypes.c_int64 * 1)(0)
     rhs = (ctypes.c_void_p * 1)(None)
-    assert lib.sgb_batch_plan_create_ex(ctypes.byref(m), rhs, ns, 1, 1, None, 1, -1, 0x1000, 1 << 20,
+    assert lib.sgb_batch_plan_create_ex(ctypes.byref(m), rhs, ns, 1, 1, None, 1, -1, 0, 0x1000, 1 << 20,
                                         ctypes.byref(plan)) == _lib.SGB_ERR_ARG
-    assert lib.sgb_batch_plan_create_ex(ctypes.byref(m), rhs, ns, 1, 1, None, 0, 24, 0x1000, 1 << 20,
+    assert lib.sgb_batch_plan_create_ex(ctypes.byref(m), rhs, ns, 1, 1, None, 0, 24, 0, 0x1000, 1 << 20,
+                                        ctypes.byref(plan)) == _lib.SGB_ERR_ARG
+    assert lib.sgb_batch_plan_create_ex(ctypes.byref(m), rhs, ns, 1, 1, None, 1, 24, 2, 0x1000, 1 << 20,
                                         ctypes.byref(plan)) == _lib.SGB_ERR_ARG
 
 

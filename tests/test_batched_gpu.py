@@ -168,10 +168,10 @@ def test_plan_panel_cta_counts_agree_with_the_oracle():
         b = int(rng.choice([96, 128]))
         mats.append(generate(n, b, 8, 2, seed=400 + i, dtype=np.float64))
     refs = [oracle_run(m) for m in mats]
-    for panel in (18, 32, 4):
+    for panel, split in ((18, False), (32, True), (4, False)):
         dev = [tuple(torch.from_numpy(x.copy()).cuda() for x in m.arrays()) for m in mats]
         rhs = [torch.from_numpy(m.B.copy()).cuda() for m in mats]
-        plan = BatchPlan(dev, rhs, nstreams=2, panel_ctas=panel)
+        plan = BatchPlan(dev, rhs, nstreams=2, panel_ctas=panel, tc_ksplit=split)
         plan.run()
         torch.cuda.synchronize()
         assert torch.all(plan.info() == 0)
@@ -188,6 +188,7 @@ def test_autotuner_returns_streams_and_panel_ctas(tmp_path, monkeypatch):
     monkeypatch.setattr(bm, "CACHE", str(tmp_path / "tune.json"))
     mats = make_batch(4, seed=12)
     dev = [tuple(torch.from_numpy(x).cuda() for x in m.arrays()) for m in mats]
-    ns, panel = bm.autotune(dev, None, ops=("pobtaf", "pobtasi"), candidates=(1, 2), panel_candidates=(18, 24))
-    assert ns in (1, 2) and panel in (0, 18)
-    assert bm.autotune(dev, None, ops=("pobtaf", "pobtasi")) == (ns, panel)  # cached
+    ns, panel, split = bm.autotune(dev, None, ops=("pobtaf", "pobtasi"), candidates=(1, 2),
+                                   panel_candidates=(18, 24))
+    assert ns in (1, 2) and panel in (0, 18) and split in (True, False)
+    assert bm.autotune(dev, None, ops=("pobtaf", "pobtasi")) == (ns, panel, split)  # cached
