@@ -462,9 +462,14 @@ struct TcSmem {
     static_assert(kStages >= 2, "at least two pipeline stages");
 };
 
-// Warp roles (192 threads): warps 0-3 epilogue (TMEM lanes 0-127), warp 4
-// producer (bulk copies into a kStages ring), warp 5 MMA issuer.
-constexpr int TC_THREADS2 = 192;
+// Warp roles (256 threads): warps 0-3 epilogue (TMEM lanes 0-127), warp 4
+// producer (bulk copies into a kStages ring), warp 5 MMA issuer; warps 6-7
+// wait for the epilogue, whose cross-CTA reduction and FP64 writes every
+// warp shares (measured at n=256, b=512, a=64: pobtaf 87.1 -> 86.3 ms,
+// pobtasi 29.8 -> 28.8 ms against six warps; the reduction's ~7 µs are
+// spent waiting on its FP64 conversions and stores, not on the distributed
+// shared-memory loads, and an integer-only conversion measured slower).
+constexpr int TC_THREADS2 = 256;  // warps 6-7 join only the epilogue
 
 template <int S, int BN>
 __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constant__ TcLaunch L) {
