@@ -462,14 +462,16 @@ struct TcSmem {
     static_assert(kStages >= 2, "at least two pipeline stages");
 };
 
-// Warp roles (256 threads): warps 0-3 epilogue (TMEM lanes 0-127), warp 4
-// producer (bulk copies into a kStages ring), warp 5 MMA issuer; warps 6-7
-// wait for the epilogue, whose cross-CTA reduction and FP64 writes every
-// warp shares (measured at n=256, b=512, a=64: pobtaf 87.1 -> 86.3 ms,
+// Warp roles (256 threads): warp 4 producer (bulk copies into a kStages
+// ring), warp 5 MMA issuer, warps 0-3 wait for the last commit; then all
+// eight warps run the epilogue -- each reads the TMEM lanes of its quarter
+// (warps w and w + 4 split the columns) -- and share the cross-CTA
+// reduction and FP64 writes (measured at n=256, b=512, a=64: pobtaf 87.1 -> 86.3 ms,
 // pobtasi 29.8 -> 28.8 ms against six warps; the reduction's ~7 µs are
 // spent waiting on its FP64 conversions and stores, not on the distributed
 // shared-memory loads, and an integer-only conversion measured slower).
 constexpr int TC_THREADS2 = 256;  // warps 6-7 join only the epilogue
+static_assert(TC_THREADS2 == 256, "the epilogue's folding splits the columns over two groups of four warps");
 
 template <int S, int BN>
 __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constant__ TcLaunch L) {
@@ -602,11 +604,11 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
     // add, power-of-two scale), staged row-major in shared memory, then
     // written out -- alpha, beta and C_in applied -- with consecutive
     // threads on consecutive columns, so global loads and stores coalesce.
+    // every warp reads TMEM in the epilogue: each observes the last commit
+    // itself, then orders its tcgen05 loads after it
     bool ok = true;
-    if (warp < 4) {
-        if (!mbar_wait(smem_u32(done), 0, L.spin)) ok = false;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    }
+    if (!mbar_wait(smem_u32(done), 0, L.spin)) ok = false;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const bool all_ok = !__syncthreads_or(!ok || flags[0] != 0);
     if (!all_ok && tid == 0 && L.err != nullptr) atomicExch(L.err, SGB_ERR_TIMEOUT);
     double* C = P.Cout + (int64_t)inst * P.strideC;
@@ -674,13 +676,16 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
         // out, consecutive threads on consecutive column pairs.
         constexpr int LD2 = BN + 2;
         float2* R2 = (float2*)smem;
-        if (all_ok && warp < 4) {
-            const int row = warp * 32 + lane;
+        if (all_ok) {
+            // every warp folds: warp w reads TMEM lanes 32 (w % 4) .. + 31, warps
+            // 0-3 the first half of the columns, warps 4-7 the second
+            const int q4 = warp & 3, half = warp >> 2;
+            const int row = q4 * 32 + lane;
 #pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += 16) {
+            for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 16) {
                 float v[NACC][16];
                 if (nkb > 0) {
-                    tmem_levels16<NACC, BN>(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+                    tmem_levels16<NACC, BN>(tmem + ((uint32_t)(q4 * 32) << 16) + c0, v);
                 } else {
 #pragma unroll
                     for (int l = 0; l < NACC; ++l)
@@ -736,14 +741,16 @@ __global__ void __launch_bounds__(TC_THREADS2, 1) k_gemm_tc(const __grid_constan
     } else {
         // the whole K here: TMEM -> FP64 tile in shared memory -> coalesced writes
         double* Ds = (double*)smem;
-        if (all_ok && warp < 4) {
-            const int row = warp * 32 + lane;
+        if (all_ok) {
+            // as above: all eight warps, two column halves
+            const int q4 = warp & 3, half = warp >> 2;
+            const int row = q4 * 32 + lane;
             const int eAm = eAs[row];
 #pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += 16) {
+            for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 16) {
                 float v[NACC][16];
                 if (nkb > 0) {
-                    tmem_levels16<NACC, BN>(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+                    tmem_levels16<NACC, BN>(tmem + ((uint32_t)(q4 * 32) << 16) + c0, v);
                 } else {
 #pragma unroll
                     for (int l = 0; l < NACC; ++l)
