@@ -560,10 +560,22 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
             if (R.cols > kTile) R.cols = kTile;
             return R;
         };
-        constexpr int U = kTile * kTile / NT;
+        // Work units: the tiles, or ns row slabs of 32 / ns rows each when
+        // every worker then has at most one (the late steps, with fewer
+        // tiles than workers).  Several slabs per CTA measured slower than
+        // one whole tile: each slab pays the staging and a barrier.
+        const int64_t ntl = total - t0;
+        const int ns = ntl * 4 <= (int64_t)nwk ? 4 : ntl * 2 <= (int64_t)nwk ? 2 : 1;
+        const int64_t units = ntl * ns;
+        // this thread's outputs in slab s: rows ro[0..nr) x columns co[0..nc)
+        // of the tile (ns = 1: 2 x 2, ns = 2: 1 x 2, ns = 4: 1 x 1)
         const int cx = tid & 15, cy = tid >> 4;
+        const int nr = ns == 1 ? 2 : 1, nc = ns == 4 ? 1 : 2;
+        auto out_row = [&](int sl, int i2) { return ns == 1 ? cy + 16 * i2 : ns == 2 ? sl * 16 + cy : sl * 8 + ty; };
+        auto out_col = [&](int j2) { return ns == 4 ? tx : cx + 16 * j2; };
+        constexpr int U = kTile * kTile / NT;
         T va[U], vb[U], vc[2][2];
-        auto fetch = [&](const TileRef& R) {
+        auto fetch = [&](const TileRef& R, int sl) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int e = tid + u * NT, r = e / kTile, k = e % kTile;
@@ -574,26 +586,28 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
             for (int i2 = 0; i2 < 2; ++i2)
 #pragma unroll
                 for (int j2 = 0; j2 < 2; ++j2) {
-                    const int r = cy + 16 * i2, c = cx + 16 * j2;
-                    vc[i2][j2] = (!R.fresh && r < R.rows && c < R.cols)
+                    const int r = out_row(sl, i2), c = out_col(j2);
+                    vc[i2][j2] = (i2 < nr && j2 < nc && !R.fresh && r < R.rows && c < R.cols)
                                      ? ldcg(R.C + (int64_t)r * R.ldc + R.cj * kTile + c)
                                      : T(0);
                 }
         };
-        int64_t t = t0 + wk;
+        int64_t u = wk;
         TileRef cur;
-        if (t < total) {
-            cur = tile_ref(t);
-            fetch(cur);
+        int cur_sl = 0;
+        if (u < units) {
+            cur = tile_ref(t0 + u / ns);
+            cur_sl = (int)(u % ns);
+            fetch(cur, cur_sl);
         }
-        for (int buf = 0; t < total; t += nwk, buf ^= 1) {
+        for (int buf = 0; u < units; u += nwk, buf ^= 1) {
             T (*As)[kTile + 1] = buf ? S.x : S.s;
             T (*Bs)[kTile + 1] = buf ? S.u : S.tmp;
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int e = tid + u * NT;
-                As[e / kTile][e % kTile] = va[u];
-                Bs[e / kTile][e % kTile] = vb[u];
+            for (int q = 0; q < U; ++q) {
+                const int e = tid + q * NT;
+                As[e / kTile][e % kTile] = va[q];
+                Bs[e / kTile][e % kTile] = vb[q];
             }
             T acc[2][2];
 #pragma unroll
@@ -602,24 +616,39 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                 for (int j2 = 0; j2 < 2; ++j2) acc[i2][j2] = vc[i2][j2];
             __syncthreads();
             const TileRef now = cur;
-            if (t + nwk < total) {  // next tile's operands in flight during this tile's FMAs
-                cur = tile_ref(t + nwk);
-                fetch(cur);
+            const int sl = cur_sl;
+            if (u + nwk < units) {  // next unit's operands in flight during this unit's FMAs
+                cur = tile_ref(t0 + (u + nwk) / ns);
+                cur_sl = (int)((u + nwk) % ns);
+                fetch(cur, cur_sl);
             }
-            for (int k = 0; k < w; ++k) {
-                const T a0 = As[cy][k], a1 = As[cy + 16][k];
-                const T b0 = Bs[cx][k], b1 = Bs[cx + 16][k];
-                acc[0][0] = fma(-a0, b0, acc[0][0]);
-                acc[0][1] = fma(-a0, b1, acc[0][1]);
-                acc[1][0] = fma(-a1, b0, acc[1][0]);
-                acc[1][1] = fma(-a1, b1, acc[1][1]);
+            if (ns == 1) {
+                for (int k = 0; k < w; ++k) {
+                    const T a0 = As[cy][k], a1 = As[cy + 16][k];
+                    const T b0 = Bs[cx][k], b1 = Bs[cx + 16][k];
+                    acc[0][0] = fma(-a0, b0, acc[0][0]);
+                    acc[0][1] = fma(-a0, b1, acc[0][1]);
+                    acc[1][0] = fma(-a1, b0, acc[1][0]);
+                    acc[1][1] = fma(-a1, b1, acc[1][1]);
+                }
+            } else if (ns == 2) {
+                const int r0 = sl * 16 + cy;
+                for (int k = 0; k < w; ++k) {
+                    const T a0 = As[r0][k];
+                    acc[0][0] = fma(-a0, Bs[cx][k], acc[0][0]);
+                    acc[0][1] = fma(-a0, Bs[cx + 16][k], acc[0][1]);
+                }
+            } else {
+                const int r0 = sl * 8 + ty;
+                for (int k = 0; k < w; ++k) acc[0][0] = fma(-As[r0][k], Bs[tx][k], acc[0][0]);
             }
 #pragma unroll
             for (int i2 = 0; i2 < 2; ++i2)
 #pragma unroll
                 for (int j2 = 0; j2 < 2; ++j2) {
-                    const int r = cy + 16 * i2, c = cx + 16 * j2;
-                    if (r < now.rows && c < now.cols) now.C[(int64_t)r * now.ldc + now.cj * kTile + c] = acc[i2][j2];
+                    const int r = out_row(sl, i2), c = out_col(j2);
+                    if (i2 < nr && j2 < nc && r < now.rows && c < now.cols)
+                        now.C[(int64_t)r * now.ldc + now.cj * kTile + c] = acc[i2][j2];
                 }
         }
         if (!group_barrier(barC, G - kW0, epC, a.status, &S.flag, a.spin)) return;
