@@ -23,12 +23,14 @@
 //                waits for the bulk update;
 //   CTA kNH+1    L writer: from M_p, d_p the tile's L into the matrix
 //                (counter I);
-//   CTAs kNH+2.. workers: the other rows below tile p (and, with xinv, the
-//                rows of L^{-T}), by the same substitution following the
-//                published columns, barrier B (with the helpers), the
-//                rank-32 update of the rest of the trailing panel (the next
-//                tile's operands and C loaded during the current tile's
-//                FMAs), barrier C (workers only).
+//   CTAs kNH+2.. workers: warps 0-3 the other rows below tile p (and, with
+//                xinv, the rows of L^{-T}), each first given its share of
+//                the trailing update of step p-1 (column block p-1 on its
+//                column block p), then the same substitution following the
+//                published columns; warps 4-7 meanwhile the rest of the
+//                trailing update of step p-1 (the next tile's operands and
+//                C loaded during the current tile's FMAs); barrier B (with
+//                the helpers).
 //
 // M, d and d^{-1/2} rotate through three buffers; the factorizer waits for
 // the L writer before overwriting one.  The two hand-offs on the chain from
@@ -72,7 +74,7 @@ struct PanelArgs {
                  // [3][32 * 32 + 32] staged columns of M and d
     int32_t* info;
     int64_t row0;
-    unsigned* bar;    // [0] F, [1] I, [4] barrier B, [6] barrier C, [8] columns of M
+    unsigned* bar;    // [0] F, [1] I, [4] barrier B, [8] columns of M
                       // published; zero at launch
     int32_t* status;  // SGB_ERR_TIMEOUT on a stuck wait
     long long spin;   // poll limit of every bounded wait
@@ -149,6 +151,12 @@ __device__ __forceinline__ bool cta_ok(const int32_t* status, int* sflag) {
     return *sflag != 0;
 }
 
+// Named barrier `id` over the first `nthreads` threads' warps (a group of
+// warps synchronizing without the rest of the CTA).
+__device__ __forceinline__ void group_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // Publish: make this CTA's global writes visible, then count on ctr (the
 // barrier orders the CTA's writes before thread 0's fence, which is
 // cumulative).
@@ -179,14 +187,16 @@ __device__ __forceinline__ T* row_ptr(const PanelArgs<T>& a, int64_t c1, int64_t
 // loaded at once.  With stage_row the result also goes to that staging row
 // (hand-off by value).  With unit >= 0
 // the row is the unit vector e_unit instead of the stored values (a row of
-// the identity, whose solve is a row of L^{-T}).  Returns false on a
-// timeout or an error raised elsewhere.
+// the identity, whose solve is a row of L^{-T}); with preset the row starts
+// from y0 (lane = column) instead.  Returns false on a timeout or an error
+// raised elsewhere.
 template <typename T>
 __device__ __forceinline__ bool trsm_row_pipe(T* rp, int w, const T* mt, const T* rv, const unsigned* colcount,
                                               unsigned col_base, int32_t* status, bool sleep, long long spin,
-                                              int unit = -1, T* stage_row = nullptr) {
+                                              int unit = -1, T* stage_row = nullptr, bool preset = false,
+                                              T y0 = T(0)) {
     const int tx = threadIdx.x & 31;
-    T y = tx < w ? (unit >= 0 ? T(tx == unit ? 1 : 0) : ldcg(rp + tx)) : T(0);
+    T y = tx < w ? (unit >= 0 ? T(tx == unit ? 1 : 0) : preset ? y0 : ldcg(rp + tx)) : T(0);
     T r = T(0);
     int k = 0;
     long long spins = 0;
@@ -338,7 +348,6 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
     unsigned* F = a.bar + 0;
     unsigned* I = a.bar + 1;
     unsigned* barB = a.bar + 4;
-    unsigned* barC = a.bar + 6;
     unsigned* CC = a.bar + 8;
     T* Mg = a.scratch;                      // [3][32*32], column k of M at [k][0..31]
     T* dg = a.scratch + 3 * kTile * kTile;  // [3][32] d
@@ -395,7 +404,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
     }
     const bool helper = cta <= (unsigned)kNH;
     const int h = (int)cta - 1;
-    unsigned epB = 0, epC = 0;
+    unsigned epB = 0;
     for (int64_t p = 0; p < nt; ++p) {
         const int64_t c0 = p * kTile;
         const int w = tile_w(p);
@@ -477,181 +486,186 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         }
 
         // ---------------- workers
-        // B(p): the rows below tile p except tile-row p+1 (the helpers'),
-        // one row per warp, following the published columns of M
-        // and, with xinv, the rows of L^{-T} that are not zero in column
-        // block p (rows < c1; those of tile-row p start as identity rows)
+        // Step p, two groups of four warps side by side:
+        //   warps 0-3  B(p): the rows below tile p except tile-row p+1 (the
+        //              helpers'), and with xinv the rows of L^{-T} not zero
+        //              in column block p (rows < c1; those of tile-row p
+        //              start as identity rows), one row per warp: first
+        //              column block p-1 applied to the row's column block p
+        //              (its share of the trailing update of step p-1), then
+        //              the substitution following the published columns of M;
+        //   warps 4-7  the rest of that trailing update: column block p-1
+        //              on the trailing panel of step p-1 without tile-rows
+        //              p, p+1 and without column block p.
+        // Then barrier B (with the helpers).  The rows never wait for the
+        // bulk update, and the bulk update runs while the rows follow the
+        // pivots.
         const unsigned nwk = G - kW0, wk = cta - kW0;
-        const int64_t off0 = w2;
-        const int64_t nbase = (m - c1) + a.r1rows + a.r2rows - off0;
-        const int64_t nrows = nbase + (a.xinv ? c1 : 0);
-        for (int64_t r = (int64_t)wk * 8 + ty; r < nrows; r += (int64_t)nwk * 8) {
-            T* rp;
-            int unit = -1;
-            if (r < nbase) {
-                rp = row_ptr(a, c1, off0 + r) + c0;
-            } else {
-                const int64_t xr = r - nbase;
-                rp = a.xinv + xr * a.xld + c0;
-                if (xr >= c0) unit = (int)(xr - c0);
+        const bool prev = p >= 1;  // the trailing update of step p-1 is due
+        if (ty < 4) {
+            const int64_t off0 = w2;
+            const int64_t nbase = (m - c1) + a.r1rows + a.r2rows - off0;
+            const int64_t nrows = nbase + (a.xinv ? c1 : 0);
+            if (prev) {  // tile-row p in column block p-1 (the helpers' rows of step p-1)
+                for (int e = tid; e < kTile * kTile; e += 128) {
+                    const int r = e / kTile, k = e % kTile;
+                    S.x[r][k] = r < w ? ldcg(a.diag + (c0 + r) * a.ldd + (c0 - kTile) + k) : T(0);
+                }
+                group_sync(1, 128);
             }
-            if (!trsm_row_pipe<T>(rp, w, Mp, rp3, CC, (unsigned)(p * kTile), a.status, true, a.spin, unit)) break;
+            for (int64_t r = (int64_t)wk * 4 + ty; r < nrows; r += (int64_t)nwk * 4) {
+                T* rp;
+                int unit = -1;
+                bool fresh = false;  // L^{-T} tile-row p-1: column block p not written yet
+                if (r < nbase) {
+                    rp = row_ptr(a, c1, off0 + r) + c0;
+                } else {
+                    const int64_t xr = r - nbase;
+                    rp = a.xinv + xr * a.xld + c0;
+                    if (xr >= c0) unit = (int)(xr - c0);
+                    else fresh = xr >= c0 - kTile;
+                }
+                T y0 = T(0);
+                if (prev && unit < 0) {  // y0 = row(block p) - row(block p-1) * (tile-row p of block p-1)^T
+                    const T av = ldcg(rp - kTile + tx);
+                    y0 = (fresh || tx >= w) ? T(0) : ldcg(rp + tx);
+#pragma unroll
+                    for (int k = 0; k < kTile; ++k) y0 = fma(-__shfl_sync(0xffffffffu, av, k), S.x[tx][k], y0);
+                }
+                if (!trsm_row_pipe<T>(rp, w, Mp, rp3, CC, (unsigned)(p * kTile), a.status, true, a.spin, unit,
+                                      nullptr, prev && unit < 0, y0))
+                    break;
+            }
+        } else if (prev) {
+            // step q = p-1: column block q, trailing panel from c1q = c0
+            const int64_t c0q = c0 - kTile, c1q = c0;
+            const int64_t ntd = (m - c1q + kTile - 1) / kTile;  // tile-rows from tile-row p
+            const int64_t n1 = (a.r1rows + kTile - 1) / kTile, n2 = (a.r2rows + kTile - 1) / kTile;
+            const int64_t nx = a.xinv ? p : 0;  // tile-rows of L^{-T} not zero in block q
+            // D tiles (ti, cj) with ti >= 2 and 1 <= cj <= ti, then the tiles
+            // of the other row sets with cj >= 1
+            const int64_t tiles_d = ntd >= 2 ? ntd * (ntd - 1) / 2 - 1 : 0;
+            const int64_t total = ntd >= 2 ? tiles_d + (n1 + n2 + nx) * (ntd - 1) : 0;
+            const T* Bpan = a.diag + c1q * a.ldd + c0q;
+            struct TileRef {
+                T* C;
+                const T* A;
+                int64_t ldc, rows, cols, cj;
+                bool fresh;  // C holds no value yet (L^{-T} tile-row q): C = -update
+            };
+            auto tile_ref = [&](int64_t t) {
+                TileRef R;
+                R.fresh = false;
+                int64_t ti;
+                if (t < tiles_d) {  // (ti - 1, cj - 1) over the triangle of ntd - 1 tile-rows, from its second tile
+                    const int64_t tt = t + 1;
+                    int64_t ui = (int64_t)((sqrt(8.0 * (double)tt + 1.0) - 1.0) * 0.5);
+                    while (ui * (ui + 1) / 2 > tt) --ui;
+                    while ((ui + 1) * (ui + 2) / 2 <= tt) ++ui;
+                    ti = ui + 1;
+                    R.cj = tt - ui * (ui + 1) / 2 + 1;
+                    R.C = a.diag + (c1q + ti * kTile) * a.ldd + c1q;
+                    R.A = a.diag + (c1q + ti * kTile) * a.ldd + c0q;
+                    R.ldc = a.ldd;
+                    R.rows = (m - c1q) - ti * kTile;
+                } else {
+                    const int64_t u = t - tiles_d;
+                    const int64_t set = u / (ntd - 1);
+                    R.cj = 1 + u % (ntd - 1);
+                    if (set < n1) {
+                        ti = set;
+                        R.C = a.r1 + ti * kTile * a.r1ld + c1q;
+                        R.A = a.r1 + ti * kTile * a.r1ld + c0q;
+                        R.ldc = a.r1ld;
+                        R.rows = a.r1rows - ti * kTile;
+                    } else if (set < n1 + n2) {
+                        ti = set - n1;
+                        R.C = a.r2 + ti * kTile * a.r2ld + c1q;
+                        R.A = a.r2 + ti * kTile * a.r2ld + c0q;
+                        R.ldc = a.r2ld;
+                        R.rows = a.r2rows - ti * kTile;
+                    } else {
+                        ti = set - n1 - n2;
+                        R.C = a.xinv + ti * kTile * a.xld + c1q;
+                        R.A = a.xinv + ti * kTile * a.xld + c0q;
+                        R.ldc = a.xld;
+                        R.rows = m - ti * kTile;
+                        R.fresh = ti == p - 1;
+                    }
+                }
+                if (R.rows > kTile) R.rows = kTile;
+                R.cols = (m - c1q) - R.cj * kTile;
+                if (R.cols > kTile) R.cols = kTile;
+                return R;
+            };
+            // 128 threads, 8 outputs each: rows cy + 8 i (i < 4), columns cx + 16 j (j < 2)
+            const int gt = tid - 128, cx = gt & 15, cy = gt >> 4;
+            constexpr int U = kTile * kTile / 128;
+            T va[U], vb[U], vc[4][2];
+            auto fetch = [&](const TileRef& R) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int e = gt + u * 128, r = e / kTile, k = e % kTile;
+                    va[u] = r < R.rows ? ldcg(R.A + (int64_t)r * R.ldc + k) : T(0);
+                    vb[u] = r < R.cols ? ldcg(Bpan + (R.cj * kTile + r) * a.ldd + k) : T(0);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        const int r = cy + 8 * i, c = cx + 16 * j;
+                        vc[i][j] = (!R.fresh && r < R.rows && c < R.cols)
+                                       ? ldcg(R.C + (int64_t)r * R.ldc + R.cj * kTile + c)
+                                       : T(0);
+                    }
+            };
+            int64_t t = wk;
+            TileRef cur;
+            if (t < total) {
+                cur = tile_ref(t);
+                fetch(cur);
+            }
+            for (; t < total; t += nwk) {
+                group_sync(2, 128);  // the previous tile's operands are no longer read
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int e = gt + u * 128;
+                    S.s[e / kTile][e % kTile] = va[u];
+                    S.tmp[e / kTile][e % kTile] = vb[u];
+                }
+                T acc[4][2];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) acc[i][j] = vc[i][j];
+                group_sync(2, 128);
+                const TileRef now = cur;
+                if (t + nwk < total) {  // next tile's operands in flight during this tile's FMAs
+                    cur = tile_ref(t + nwk);
+                    fetch(cur);
+                }
+                for (int k = 0; k < kTile; ++k) {
+                    T av[4], bv[2];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) av[i] = S.s[cy + 8 * i][k];
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) bv[j] = S.tmp[cx + 16 * j][k];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) acc[i][j] = fma(-av[i], bv[j], acc[i][j]);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        const int r = cy + 8 * i, c = cx + 16 * j;
+                        if (r < now.rows && c < now.cols) now.C[(int64_t)r * now.ldc + now.cj * kTile + c] = acc[i][j];
+                    }
+            }
         }
         if (!has_next) break;
         if (!group_barrier(barB, G - 2, epB, a.status, &S.flag, a.spin)) return;
-
-        // C(p): rank-w update of the trailing panel without tile-rows p+1, p+2
-        const int64_t ntd = (m - c1 + kTile - 1) / kTile;
-        const int64_t n1 = (a.r1rows + kTile - 1) / kTile, n2 = (a.r2rows + kTile - 1) / kTile;
-        const int64_t nx = a.xinv ? p + 1 : 0;  // tile-rows of L^{-T} not zero in block p
-        const int64_t tiles_d = ntd * (ntd + 1) / 2;
-        const int64_t total = tiles_d + (n1 + n2 + nx) * ntd;
-        const int64_t t0 = tiles_d < 3 ? tiles_d : 3;
-        const T* Bpan = a.diag + c1 * a.ldd + c0;
-        // Tile t's operands are staged in one of two shared buffers while
-        // tile t+nwk's are being loaded into registers.
-        struct TileRef {
-            T* C;
-            const T* A;
-            int64_t ldc, rows, cols, cj;
-            bool fresh;  // C holds no value yet (L^{-T} tile-row p): C = -update
-        };
-        auto tile_ref = [&](int64_t t) {
-            TileRef R;
-            R.fresh = false;
-            int64_t ti;
-            if (t < tiles_d) {  // lower tiles of the trailing D, row-major over the triangle
-                ti = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-                while (ti * (ti + 1) / 2 > t) --ti;
-                while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-                R.cj = t - ti * (ti + 1) / 2;
-                R.C = a.diag + (c1 + ti * kTile) * a.ldd + c1;
-                R.A = a.diag + (c1 + ti * kTile) * a.ldd + c0;
-                R.ldc = a.ldd;
-                R.rows = (m - c1) - ti * kTile;
-            } else if (t < tiles_d + n1 * ntd) {
-                const int64_t u = t - tiles_d;
-                ti = u / ntd;
-                R.cj = u % ntd;
-                R.C = a.r1 + ti * kTile * a.r1ld + c1;
-                R.A = a.r1 + ti * kTile * a.r1ld + c0;
-                R.ldc = a.r1ld;
-                R.rows = a.r1rows - ti * kTile;
-            } else if (t < tiles_d + (n1 + n2) * ntd) {
-                const int64_t u = t - tiles_d - n1 * ntd;
-                ti = u / ntd;
-                R.cj = u % ntd;
-                R.C = a.r2 + ti * kTile * a.r2ld + c1;
-                R.A = a.r2 + ti * kTile * a.r2ld + c0;
-                R.ldc = a.r2ld;
-                R.rows = a.r2rows - ti * kTile;
-            } else {
-                const int64_t u = t - tiles_d - (n1 + n2) * ntd;
-                ti = u / ntd;
-                R.cj = u % ntd;
-                R.C = a.xinv + ti * kTile * a.xld + c1;
-                R.A = a.xinv + ti * kTile * a.xld + c0;
-                R.ldc = a.xld;
-                R.rows = m - ti * kTile;
-                R.fresh = ti == p;
-            }
-            if (R.rows > kTile) R.rows = kTile;
-            R.cols = (m - c1) - R.cj * kTile;
-            if (R.cols > kTile) R.cols = kTile;
-            return R;
-        };
-        // Work units: the tiles, or ns row slabs of 32 / ns rows each when
-        // every worker then has at most one (the late steps, with fewer
-        // tiles than workers).  Several slabs per CTA measured slower than
-        // one whole tile: each slab pays the staging and a barrier.
-        const int64_t ntl = total - t0;
-        const int ns = ntl * 4 <= (int64_t)nwk ? 4 : ntl * 2 <= (int64_t)nwk ? 2 : 1;
-        const int64_t units = ntl * ns;
-        // this thread's outputs in slab s: rows ro[0..nr) x columns co[0..nc)
-        // of the tile (ns = 1: 2 x 2, ns = 2: 1 x 2, ns = 4: 1 x 1)
-        const int cx = tid & 15, cy = tid >> 4;
-        const int nr = ns == 1 ? 2 : 1, nc = ns == 4 ? 1 : 2;
-        auto out_row = [&](int sl, int i2) { return ns == 1 ? cy + 16 * i2 : ns == 2 ? sl * 16 + cy : sl * 8 + ty; };
-        auto out_col = [&](int j2) { return ns == 4 ? tx : cx + 16 * j2; };
-        constexpr int U = kTile * kTile / NT;
-        T va[U], vb[U], vc[2][2];
-        auto fetch = [&](const TileRef& R, int sl) {
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int e = tid + u * NT, r = e / kTile, k = e % kTile;
-                va[u] = (r < R.rows && k < w) ? ldcg(R.A + (int64_t)r * R.ldc + k) : T(0);
-                vb[u] = (r < R.cols && k < w) ? ldcg(Bpan + (R.cj * kTile + r) * a.ldd + k) : T(0);
-            }
-#pragma unroll
-            for (int i2 = 0; i2 < 2; ++i2)
-#pragma unroll
-                for (int j2 = 0; j2 < 2; ++j2) {
-                    const int r = out_row(sl, i2), c = out_col(j2);
-                    vc[i2][j2] = (i2 < nr && j2 < nc && !R.fresh && r < R.rows && c < R.cols)
-                                     ? ldcg(R.C + (int64_t)r * R.ldc + R.cj * kTile + c)
-                                     : T(0);
-                }
-        };
-        int64_t u = wk;
-        TileRef cur;
-        int cur_sl = 0;
-        if (u < units) {
-            cur = tile_ref(t0 + u / ns);
-            cur_sl = (int)(u % ns);
-            fetch(cur, cur_sl);
-        }
-        for (int buf = 0; u < units; u += nwk, buf ^= 1) {
-            T (*As)[kTile + 1] = buf ? S.x : S.s;
-            T (*Bs)[kTile + 1] = buf ? S.u : S.tmp;
-#pragma unroll
-            for (int q = 0; q < U; ++q) {
-                const int e = tid + q * NT;
-                As[e / kTile][e % kTile] = va[q];
-                Bs[e / kTile][e % kTile] = vb[q];
-            }
-            T acc[2][2];
-#pragma unroll
-            for (int i2 = 0; i2 < 2; ++i2)
-#pragma unroll
-                for (int j2 = 0; j2 < 2; ++j2) acc[i2][j2] = vc[i2][j2];
-            __syncthreads();
-            const TileRef now = cur;
-            const int sl = cur_sl;
-            if (u + nwk < units) {  // next unit's operands in flight during this unit's FMAs
-                cur = tile_ref(t0 + (u + nwk) / ns);
-                cur_sl = (int)((u + nwk) % ns);
-                fetch(cur, cur_sl);
-            }
-            if (ns == 1) {
-                for (int k = 0; k < w; ++k) {
-                    const T a0 = As[cy][k], a1 = As[cy + 16][k];
-                    const T b0 = Bs[cx][k], b1 = Bs[cx + 16][k];
-                    acc[0][0] = fma(-a0, b0, acc[0][0]);
-                    acc[0][1] = fma(-a0, b1, acc[0][1]);
-                    acc[1][0] = fma(-a1, b0, acc[1][0]);
-                    acc[1][1] = fma(-a1, b1, acc[1][1]);
-                }
-            } else if (ns == 2) {
-                const int r0 = sl * 16 + cy;
-                for (int k = 0; k < w; ++k) {
-                    const T a0 = As[r0][k];
-                    acc[0][0] = fma(-a0, Bs[cx][k], acc[0][0]);
-                    acc[0][1] = fma(-a0, Bs[cx + 16][k], acc[0][1]);
-                }
-            } else {
-                const int r0 = sl * 8 + ty;
-                for (int k = 0; k < w; ++k) acc[0][0] = fma(-As[r0][k], Bs[tx][k], acc[0][0]);
-            }
-#pragma unroll
-            for (int i2 = 0; i2 < 2; ++i2)
-#pragma unroll
-                for (int j2 = 0; j2 < 2; ++j2) {
-                    const int r = out_row(sl, i2), c = out_col(j2);
-                    if (i2 < nr && j2 < nc && r < now.rows && c < now.cols)
-                        now.C[(int64_t)r * now.ldc + now.cj * kTile + c] = acc[i2][j2];
-                }
-        }
-        if (!group_barrier(barC, G - kW0, epC, a.status, &S.flag, a.spin)) return;
     }
 }
 
