@@ -262,6 +262,9 @@ __device__ __forceinline__ bool trsm_row_vals(T* rp, int w, const T* vc, int32_t
         decltype(Staged<T>::ld(vc)) raw[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) raw[u] = u < nb ? Staged<T>::ld(vc + (k + u) * kTile + tx) : Staged<T>::kSentinel;
+        // this lane's pivot in the same round (staged before its column;
+        // polled below only if it has not landed yet)
+        const auto rd = (tx >= k && tx < k + nb) ? Staged<T>::ld(vc + kTile * kTile + tx) : Staged<T>::kSentinel;
         int navail = 0;
 #pragma unroll
         for (int u = 0; u < 8; ++u)
@@ -282,11 +285,15 @@ __device__ __forceinline__ bool trsm_row_vals(T* rp, int w, const T* vc, int32_t
         }
         if (tx >= k && tx < k + navail) {
             T d;
-            const T* dp[1] = {vc + kTile * kTile + tx};
-            const bool want[1] = {true};
-            T dv[1];
-            if (!stage_take<T, 1>(dp, want, dv, spin, status)) atomicExch(status, SGB_ERR_TIMEOUT);
-            d = dv[0];
+            if (rd != Staged<T>::kSentinel) {
+                d = Staged<T>::val(rd);
+            } else {
+                const T* dp[1] = {vc + kTile * kTile + tx};
+                const bool want[1] = {true};
+                T dv[1];
+                if (!stage_take<T, 1>(dp, want, dv, spin, status)) atomicExch(status, SGB_ERR_TIMEOUT);
+                d = dv[0];
+            }
             r = rsq<T>(d);
         }
         k += navail;
