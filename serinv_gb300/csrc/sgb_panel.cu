@@ -29,8 +29,9 @@
 //                column block p), then the same substitution following the
 //                published columns; warps 4-7 meanwhile the rest of the
 //                trailing update of step p-1 (the next tile's operands and
-//                C loaded during the current tile's FMAs); barrier B (with
-//                the helpers).
+//                C loaded during the current tile's FMAs), then they take
+//                rows too (a per-CTA row counter); barrier B (with the
+//                helpers).
 //
 // M, d and d^{-1/2} rotate through three buffers; the factorizer waits for
 // the L writer before overwriting one.  The two hand-offs on the chain from
@@ -412,6 +413,8 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
     const bool helper = cta <= (unsigned)kNH;
     const int h = (int)cta - 1;
     unsigned epB = 0;
+    if (tid == 0) S.rowq[0] = S.rowq[1] = 0;
+    __syncthreads();
     for (int64_t p = 0; p < nt; ++p) {
         const int64_t c0 = p * kTile;
         const int w = tile_w(p);
@@ -509,39 +512,61 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         // pivots.
         const unsigned nwk = G - kW0, wk = cta - kW0;
         const bool prev = p >= 1;  // the trailing update of step p-1 is due
+        const int64_t off0 = w2;
+        const int64_t nbase = (m - c1) + a.r1rows + a.r2rows - off0;
+        const int64_t nrows = nbase + (a.xinv ? c1 : 0);
+        if (tid == 0) S.rowq[(p + 1) & 1] = 0;  // the next step's row counter (used after barrier B)
+        // This CTA's q-th row of the step: wk*4 + (q & 3) + (q / 4) * nwk*4.
+        // Warps 0-3 start with q = ty and take every further q from a shared
+        // counter; when the rows outnumber the first round (the tall panels
+        // of the FP64 forms), warps 4-7 join once their share of the update
+        // is done, with their own copy of the tile-row operand.
+        const bool tall = nrows > (int64_t)nwk * 4;
+        // tile-row p in column block p-1 (the helpers' rows of step p-1),
+        // the operand of every row's share of the update: to S.x (warps
+        // 0-3) or S.u (warps 4-7)
+        auto load_tile_row = [&](T (*dst)[kTile + 1], int gt) {
+            for (int e = gt; e < kTile * kTile; e += 128) {
+                const int r = e / kTile, k = e % kTile;
+                dst[r][k] = r < w ? ldcg(a.diag + (c0 + r) * a.ldd + (c0 - kTile) + k) : T(0);
+            }
+        };
+        auto row_of = [&](int64_t q) { return (int64_t)wk * 4 + (q & 3) + (q >> 2) * (int64_t)nwk * 4; };
+        auto next_q = [&]() -> int64_t {
+            int g = 0;
+            if (tx == 0) g = atomicAdd(&S.rowq[p & 1], 1);
+            return 4 + (int64_t)__shfl_sync(0xffffffffu, g, 0);
+        };
+        auto do_row = [&](int64_t r, T (*tr)[kTile + 1]) -> bool {
+            T* rp;
+            int unit = -1;
+            bool fresh = false;  // L^{-T} tile-row p-1: column block p not written yet
+            if (r < nbase) {
+                rp = row_ptr(a, c1, off0 + r) + c0;
+            } else {
+                const int64_t xr = r - nbase;
+                rp = a.xinv + xr * a.xld + c0;
+                if (xr >= c0) unit = (int)(xr - c0);
+                else fresh = xr >= c0 - kTile;
+            }
+            T y0 = T(0);
+            if (prev && unit < 0) {  // y0 = row(block p) - row(block p-1) * (tile-row p of block p-1)^T
+                const T av = ldcg(rp - kTile + tx);
+                y0 = (fresh || tx >= w) ? T(0) : ldcg(rp + tx);
+#pragma unroll
+                for (int k = 0; k < kTile; ++k) y0 = fma(-__shfl_sync(0xffffffffu, av, k), tr[tx][k], y0);
+            }
+            return trsm_row_pipe<T>(rp, w, Mp, rp3, CC, (unsigned)(p * kTile), a.status, true, a.spin, unit, nullptr,
+                                    prev && unit < 0, y0);
+        };
         if (ty < 4) {
-            const int64_t off0 = w2;
-            const int64_t nbase = (m - c1) + a.r1rows + a.r2rows - off0;
-            const int64_t nrows = nbase + (a.xinv ? c1 : 0);
-            if (prev) {  // tile-row p in column block p-1 (the helpers' rows of step p-1)
-                for (int e = tid; e < kTile * kTile; e += 128) {
-                    const int r = e / kTile, k = e % kTile;
-                    S.x[r][k] = r < w ? ldcg(a.diag + (c0 + r) * a.ldd + (c0 - kTile) + k) : T(0);
-                }
+            if (prev) {
+                load_tile_row(S.x, tid);
                 group_sync(1, 128);
             }
-            for (int64_t r = (int64_t)wk * 4 + ty; r < nrows; r += (int64_t)nwk * 4) {
-                T* rp;
-                int unit = -1;
-                bool fresh = false;  // L^{-T} tile-row p-1: column block p not written yet
-                if (r < nbase) {
-                    rp = row_ptr(a, c1, off0 + r) + c0;
-                } else {
-                    const int64_t xr = r - nbase;
-                    rp = a.xinv + xr * a.xld + c0;
-                    if (xr >= c0) unit = (int)(xr - c0);
-                    else fresh = xr >= c0 - kTile;
-                }
-                T y0 = T(0);
-                if (prev && unit < 0) {  // y0 = row(block p) - row(block p-1) * (tile-row p of block p-1)^T
-                    const T av = ldcg(rp - kTile + tx);
-                    y0 = (fresh || tx >= w) ? T(0) : ldcg(rp + tx);
-#pragma unroll
-                    for (int k = 0; k < kTile; ++k) y0 = fma(-__shfl_sync(0xffffffffu, av, k), S.x[tx][k], y0);
-                }
-                if (!trsm_row_pipe<T>(rp, w, Mp, rp3, CC, (unsigned)(p * kTile), a.status, true, a.spin, unit,
-                                      nullptr, prev && unit < 0, y0))
-                    break;
+            for (int64_t q = ty;; q = next_q()) {
+                const int64_t r = row_of(q);
+                if (r >= nrows || !do_row(r, S.x)) break;
             }
         } else if (prev) {
             // step q = p-1: column block q, trailing panel from c1q = c0
@@ -669,6 +694,16 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
                         const int r = cy + 8 * i, c = cx + 16 * j;
                         if (r < now.rows && c < now.cols) now.C[(int64_t)r * now.ldc + now.cj * kTile + c] = acc[i][j];
                     }
+            }
+        }
+        if (ty >= 4 && tall) {  // the update's share done: help with the rows still left
+            if (prev) {
+                load_tile_row(S.u, tid - 128);
+                group_sync(2, 128);
+            }
+            for (;;) {
+                const int64_t r = row_of(next_q());
+                if (r >= nrows || !do_row(r, S.u)) break;
             }
         }
         if (!has_next) break;

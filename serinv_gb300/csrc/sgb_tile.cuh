@@ -43,7 +43,8 @@ struct Smem {
     unsigned short tri[kTile * (kTile + 1) / 2];  // (row << 8) | col of the lower triangle, row-major
     int fail;
     int flag;
-    int pub;  // factor_tile_m: columns the companion has completed
+    int pub;      // factor_tile_m: columns the companion has completed
+    int rowq[2];  // column-block kernel workers: row counters of alternate steps
 };
 
 // Recursive-doubling inverse of the (identity padded) lower tile s into x.
