@@ -500,13 +500,16 @@ __global__ void __launch_bounds__(NT, 1) k_factor_panel(const __grid_constant__ 
         //   warps 0-3  B(p): the rows below tile p except tile-row p+1 (the
         //              helpers'), and with xinv the rows of L^{-T} not zero
         //              in column block p (rows < c1; those of tile-row p
-        //              start as identity rows), one row per warp: first
-        //              column block p-1 applied to the row's column block p
-        //              (its share of the trailing update of step p-1), then
-        //              the substitution following the published columns of M;
+        //              start as identity rows), one row at a time per
+        //              warp: first column block p-1 applied to the row's
+        //              column block p
+        //              (its share of the trailing update of step p-1),
+        //              then the substitution following the published
+        //              columns of M;
         //   warps 4-7  the rest of that trailing update: column block p-1
         //              on the trailing panel of step p-1 without tile-rows
-        //              p, p+1 and without column block p.
+        //              p, p+1 and without column block p; then rows as well
+        //              in tall panels.
         // Then barrier B (with the helpers).  The rows never wait for the
         // bulk update, and the bulk update runs while the rows follow the
         // pivots.
